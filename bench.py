@@ -1,0 +1,294 @@
+#!/usr/bin/env python3
+"""Throughput of the explicit unstructured FV update on GB300.
+
+Workload (default): the Mach 2.5 supersonic wedge -- [0,3]x[0,1] with a 15-degree
+ramp from x=0.5, ~1.0M seeded-Delaunay triangles graded 2x toward the ramp (seed 0),
+Rusanov flux, limited second order, RK2 at CFL 0.4, plain FP64.  A step is one RK2
+time step of the whole mesh (two residual evaluations + stage updates + the
+per-step reductions of the time loop); the metric is cell-updates/s = cells x
+steps / time.  The ~1M-cell state and face arrays (~0.5 GB) exceed the 129 MB L2,
+so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference-semantics FP64 CPU restatement (oracle/) on all
+host cores on the same mesh and config (the D reference cannot be built on this
+machine or the GPU host: no D compiler, MPI or ParMETIS).  N>1: one independent
+replica per GPU (the path does not shard), weak scaling.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WEDGE_BCS = [{"tag": "Inflow", "type": "fullState", "q": [2.5, 0, 1, 1]},
+             {"tag": "Top", "type": "fullState", "q": [2.5, 0, 1, 1]},
+             {"tag": "Symmetry", "type": "symmetry", "q": [2.5, 0, 1, 1]},
+             {"tag": "Ramp", "type": "inviscidWall", "q": [2.5, 0, 1, 1]},
+             {"tag": "Outflow", "type": "fullState", "q": [2.5, 0, 1, 1]}]
+
+
+def wedge_config(cfl=0.4):
+    return json.dumps({"mesh": "wedge.msh", "dt": 1e-4, "tEnd": 1e9, "flux": "rusanovFlux", "saveIter": -1,
+                       "plotIter": -1, "forceBoundary": "Ramp", "integrator": "RK2", "limited": True, "CFL": cfl,
+                       "initialConditions": [2.5, 0, 1, 1], "boudaryConditions": WEDGE_BCS})
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.p = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        rows = []
+        for line in open(self.f.name):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if "Active" in r[5 + k]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def algorithmic_bytes(info, need_grad=False, limited=True):
+    """Bytes each kernel must move per launch, every array touched once (re-reads of
+    a neighbour's state count 0).  S = face slots, E = interior edges, G = boundary edges."""
+    C, S, E, G = info.n_cells, info.face_slots, info.n_int_edges, info.n_ghost
+    cell = C * (32 + 4) + S * (4 + 16 + (16 if limited else 0) + 16) + S * 32 + (C * 64 if need_grad else 0)
+    flux = E * (8 + 16 + 8 + 64 + 40) + G * (12 + 16 + 8 + 32 + 32 + 40)
+    # residual + RK2 first-stage update: per cell nedge, perim, d, -1/area, q read, aux and stage-state writes
+    update = C * (4 + 24 + 32 + 32 + 32) + S * 4 + (E + G) * 40
+    return {"cell": cell, "flux": flux, "update": update}
+
+
+def run_ours(args, ws, rank, local):
+    import ctypes as C
+    import ebbcfd_gb300 as E
+    from ebbcfd_gb300 import _lib, meshgen
+
+    L = _lib.load()
+    L.ebb_set_device(local)
+    t0 = time.time()
+    gen = meshgen.wedge(args.cells, seed=0)
+    mesh = gen.to_solver_mesh()
+    cfg = E.load_config(wedge_config())
+    sol = E.UfvmSolver(mesh, cfg)
+    setup_s = time.time() - t0
+    info = mesh.info
+    ncell = info.n_cells
+
+    # warm-up (also builds the CUDA graphs of the time loop)
+    sol.run(args.warmup, records=False)
+
+    # per-kernel device times (CUDA events on the solver stream)
+    ms = (C.c_double * 4)()
+    L.ebb_profile_kernels(sol.h, 20, ms)
+    kern_ms = {"cell": ms[0], "flux": ms[1], "update": ms[2], "step_end": ms[3]}
+
+    barrier = None
+    if ws > 1:
+        import torch.distributed as dist
+        barrier = dist.barrier
+        barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    n = C.c_int64()
+    dev_ms = C.c_double()
+    code = L.ebb_run_timed(sol.h, args.steps, C.byref(n), C.byref(dev_ms))
+    clk = clocks.stop()
+    if code != 0:
+        sol._raise(code)
+    if barrier:
+        barrier()
+    elapsed = dev_ms.value / 1e3
+    steps_done = n.value
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([elapsed], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    value = ws * ncell * steps_done / elapsed
+
+    # end to end through the public API with host buffers: every step uploads the state
+    # from page-locked memory, advances one step and reads the state and step record back
+    e2e = None
+    if not args.no_e2e:
+        nbytes = ncell * 4 * 8
+        ph = C.c_void_p()
+        L.ebb_host_alloc(nbytes, C.byref(ph))
+        host = np.ctypeslib.as_array((C.c_double * (ncell * 4)).from_address(ph.value)).reshape(ncell, 4)
+        L.ebb_get_state(sol.h, host.ctypes.data_as(C.POINTER(C.c_double)))
+        rec = (_lib.StepRecord * 1)()
+        k_e2e = max(3, min(args.steps, 50))
+        hp = host.ctypes.data_as(C.POINTER(C.c_double))
+        t1 = time.perf_counter()
+        for _ in range(k_e2e):
+            L.ebb_set_state(sol.h, hp)
+            L.ebb_run(sol.h, 1, rec, C.byref(n))
+            L.ebb_get_state(sol.h, hp)
+        t_e2e = time.perf_counter() - t1
+        L.ebb_host_free(ph)
+        e2e = {"value": ws * ncell * k_e2e / t_e2e, "unit": "cell-updates/s", "h2d_bytes_per_step": nbytes,
+               "d2h_bytes_per_step": nbytes + C.sizeof(_lib.StepRecord), "steps": k_e2e}
+
+    peak, peak_kind = peaks()
+    ab = algorithmic_bytes(info)
+    dom = max(("cell", "flux", "update"), key=lambda k: kern_ms[k])
+    achieved = ab[dom] / (kern_ms[dom] * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": "k_" + dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+            "kernel_ms": kern_ms, "algorithmic_bytes": ab}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(gen, ncell, budget_s=args.cpu_budget)
+
+    out = {
+        "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": steps_done,
+        "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / max(1, steps_done), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "wedge-M2.5-rusanov-rk2-cfl0.4", "cells": ncell, "faces": info.face_slots,
+                   "interior_edges": info.n_int_edges, "boundary_edges": info.n_ghost, "precision": "plain-fp64",
+                   "l2": "inputs larger than L2 (~%d MB resident)" % (sol_bytes(info) // 2 ** 20),
+                   "parallelism": "replicas" if ws > 1 else "single", "setup_s": round(setup_s, 2)},
+        "cell_stages_per_s": 2 * value, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+        "gpu_launches": steps_done * 7, "clocks": clk,
+    }
+    return out
+
+
+def sol_bytes(info):
+    C, S, E, G = info.n_cells, info.face_slots, info.n_int_edges, info.n_ghost
+    return 8 * (12 * (C + G) + 4 * 4 * S // 3 + 8 * (C + G) + 5 * (E + G) + 12 * S)
+
+
+def cpu_baseline(gen, ncell, budget_s=20.0, steps_max=1000):
+    from oracle import gmsh_ref, ref
+    nthreads = ref.max_threads()
+    ref.set_threads(nthreads)
+    om = ref.OracleMesh(gen.as_reader_dict(), gmsh_ref.load_config(wedge_config()))
+    t0 = time.perf_counter()
+    om.run(1)
+    t1 = time.perf_counter() - t0
+    n = int(max(1, min(steps_max, budget_s / max(t1, 1e-6))))
+    t0 = time.perf_counter()
+    om.run(n)
+    t = time.perf_counter() - t0
+    ref.set_threads(1)
+    return {"value": ncell * n / t, "unit": "cell-updates/s", "cores": nthreads, "kind": "port",
+            "sample": "%d RK2 steps of the full %d-cell wedge (after 1 untimed step)" % (n, ncell)}
+
+
+def run_reference(args, ws, rank):
+    from ebbcfd_gb300 import meshgen
+    from oracle import gmsh_ref, ref
+    gen = meshgen.wedge(args.cells, seed=0)
+    nthreads = ref.max_threads()
+    ref.set_threads(nthreads)
+    om = ref.OracleMesh(gen.as_reader_dict(), gmsh_ref.load_config(wedge_config()))
+    ncell = om.n_cells
+    om.run(args.warmup)
+    t0 = time.perf_counter()
+    om.run(1)
+    t1 = time.perf_counter() - t0
+    n = int(max(1, min(args.steps, args.cpu_budget * 4 / max(t1, 1e-6))))
+    t0 = time.perf_counter()
+    if n > 1:
+        om.run(n - 1)
+    t = time.perf_counter() - t0 + t1
+    v = ncell * n / t
+    return {"impl": "reference", "metric": "cell-updates/s", "value": v, "unit": "cell-updates/s", "n_gpus": ws,
+            "steps": n, "warmup": args.warmup, "ms_per_step": 1e3 * t / n, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "wedge-M2.5-rusanov-rk2-cfl0.4", "cells": ncell, "precision": "plain-fp64"},
+            "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": nthreads, "kind": "port",
+                             "sample": "%d of %d requested RK2 steps of the full %d-cell wedge" % (n, args.steps,
+                                                                                                   ncell)},
+            "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cells", type=int, default=1_000_000)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args, ws, rank)))
+        return
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    out = run_ours(args, ws, rank, local)
+    if rank == 0:
+        print(json.dumps(out))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

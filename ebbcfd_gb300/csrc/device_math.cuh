@@ -1,0 +1,225 @@
+// device_math.cuh -- per-face and per-cell arithmetic of the explicit FV update,
+// templated on the arithmetic type T (double for the plain path, float for the
+// split path).  Every expression keeps the evaluation order of the D reference so
+// that, compiled without multiply-add contraction, the double instantiation rounds
+// exactly like it.  Reference lines are cited per function.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+namespace ebbdev {
+
+// gamma is an immutable 1.4 (source/euler.d:89)
+template <typename T> struct K;
+template <> struct K<double> {
+    static constexpr double g = 1.4, gm1 = 1.4 - 1, gm1d = 1.4 - 1.0;
+};
+template <> struct K<float> {
+    static constexpr float g = 1.4f, gm1 = 1.4f - 1, gm1d = 1.4f - 1.0f;
+};
+
+template <typename T> __device__ __forceinline__ T dsqrt(T x) { return sqrt(x); }
+template <> __device__ __forceinline__ float dsqrt<float>(float x) { return sqrtf(x); }
+
+// source/euler.d:91-94
+template <typename T> __device__ __forceinline__ T pressure(const T q[4])
+{
+    T a = q[1] / q[0], b = q[2] / q[0];
+    return K<T>::gm1 * (q[3] - T(0.5) * q[0] * (a * a + b * b));
+}
+
+// source/flux.d:19-24
+template <typename T>
+__device__ __forceinline__ void convective_flux(T p, T u, T v, T rho, T e, T nx, T ny, T out[4])
+{
+    T f0 = rho * u, f1 = p + rho * (u * u), f2 = rho * u * v, f3 = u * (p + e);
+    T h0 = rho * v, h1 = rho * u * v, h2 = p + rho * (v * v), h3 = v * (p + e);
+    out[0] = f0 * nx + h0 * ny;
+    out[1] = f1 * nx + h1 * ny;
+    out[2] = f2 * nx + h2 * ny;
+    out[3] = f3 * nx + h3 * ny;
+}
+
+template <typename T> __device__ __forceinline__ T entropy_fix(T lam, T eps)
+{
+    if (lam < eps) lam = (eps * eps + lam * lam) / (T(2.0) * eps);
+    return lam;
+}
+
+template <typename T> __device__ __forceinline__ T max4(T a, T b, T c, T d)
+{
+    T m = a;
+    if (b > m) m = b;
+    if (c > m) m = c;
+    if (d > m) m = d;
+    return m;
+}
+
+// source/flux.d:224-303
+template <typename T>
+__device__ __forceinline__ void roe_flux(const T qL[4], const T qR[4], T nx, T ny, T out[4], T &sMax)
+{
+    const T gm1 = K<T>::gm1;
+    T rhoL = qL[0], uL = qL[1] / rhoL, vL = qL[2] / rhoL;
+    T rvL0 = rhoL * uL, rvL1 = rhoL * vL;
+    T pL = gm1 * (qL[3] - T(0.5) * rhoL * (uL * uL + vL * vL));
+    T hL = (qL[3] + pL) / rhoL;
+    T rhoR = qR[0], uR = qR[1] / rhoR, vR = qR[2] / rhoR;
+    T rvR0 = rhoR * uR, rvR1 = rhoR * vR;
+    T pR = gm1 * (qR[3] - T(0.5) * rhoR * (uR * uR + vR * vR));
+    T hR = (qR[3] + pR) / rhoR;
+
+    T di = dsqrt(rhoR / rhoL);
+    T d1 = T(1.0) / (T(1.0) + di);
+    T vel0 = (di * uR + uL) * d1;
+    T vel1 = (di * vR + vL) * d1;
+    T u = vel0 * nx + vel1 * ny;
+    T h = (di * hR + hL) * d1;
+    T a = dsqrt(K<T>::gm1d * (h - T(0.5) * (vel0 * vel0 + vel1 * vel1)));
+
+    T dRV0 = rvR0 - rvL0, dRV1 = rvR1 - rvL1;
+    T dRho = rhoR - rhoL;
+    T dRhoE = qR[3] - qL[3];
+
+    T lam1 = fabs(u + a), lam2 = fabs(u - a), lam3 = fabs(u);
+    T eps = T(0.01) * a;
+    lam1 = entropy_fix(lam1, eps);
+    lam2 = entropy_fix(lam2, eps);
+    lam3 = entropy_fix(lam3, eps);
+    sMax = max4(fabs(lam1), fabs(lam2), fabs(lam3), fabs(lam3));
+
+    T s1 = T(0.5) * (lam1 + lam2);
+    T s2 = T(0.5) * (lam1 - lam2);
+    T qq = dsqrt(vel0 * vel0 + vel1 * vel1);
+    T G1 = gm1 * (((qq * qq) / T(2.0)) * dRho - (vel0 * dRV0 + vel1 * dRV1) + dRhoE);
+    T G2 = -u * dRho + (dRV0 * nx + dRV1 * ny);
+    T C1 = (G1 / (a * a)) * (s1 - lam3) + G2 / a * s2;
+    T C2 = (G1 / a) * s2 + (s1 - lam3) * G2;
+
+    T fL[4], fR[4];
+    convective_flux(pL, uL, vL, rhoL, qL[3], nx, ny, fL);
+    convective_flux(pR, uR, vR, rhoR, qR[3], nx, ny, fR);
+    T D0 = lam3 * dRho + C1;
+    T D1 = lam3 * dRV0 + C1 * vel0 + C2 * nx;
+    T D2 = lam3 * dRV1 + C1 * vel1 + C2 * ny;
+    T D3 = lam3 * dRhoE + C1 * h + C2 * u;
+    out[0] = T(0.5) * (fL[0] + fR[0]) - T(0.5) * D0;
+    out[1] = T(0.5) * (fL[1] + fR[1]) - T(0.5) * D1;
+    out[2] = T(0.5) * (fL[2] + fR[2]) - T(0.5) * D2;
+    out[3] = T(0.5) * (fL[3] + fR[3]) - T(0.5) * D3;
+}
+
+// source/flux.d:66-141 (Roe-type averaged speed; every wave set to sMax)
+template <typename T>
+__device__ __forceinline__ void rusanov_flux(const T qL[4], const T qR[4], T nx, T ny, T out[4], T &sMax)
+{
+    const T gm1 = K<T>::gm1;
+    T rhoL = qL[0], uL = qL[1] / rhoL, vL = qL[2] / rhoL;
+    T rvL0 = rhoL * uL, rvL1 = rhoL * vL;
+    T pL = gm1 * (qL[3] - T(0.5) * rhoL * (uL * uL + vL * vL));
+    T hL = (qL[3] + pL) / rhoL;
+    T rhoR = qR[0], uR = qR[1] / rhoR, vR = qR[2] / rhoR;
+    T rvR0 = rhoR * uR, rvR1 = rhoR * vR;
+    T pR = gm1 * (qR[3] - T(0.5) * rhoR * (uR * uR + vR * vR));
+    T hR = (qR[3] + pR) / rhoR;
+
+    T rho = dsqrt(rhoL * rhoR);
+    T sL = dsqrt(rhoL), sR = dsqrt(rhoR);
+    T vel0 = (sL * uL + sR * uR) / (sL + sR);
+    T vel1 = (sL * vL + sR * vR) / (sL + sR);
+    T u = vel0 * nx + vel1 * ny;
+    T p = (sL * pL + sR * pR) / (sL + sR);
+    T h = (sL * hL + sR * hR) / (sL + sR);
+    T a = dsqrt(K<T>::g * (p / rho));
+
+    T dRV0 = rvR0 - rvL0, dRV1 = rvR1 - rvL1;
+    T dRho = rhoR - rhoL;
+    T dRhoE = qR[3] - qL[3];
+
+    T lam1 = fabs(u + a), lam2 = fabs(u - a), lam3 = fabs(u);
+    T eps = T(0.01) * a;
+    lam1 = entropy_fix(lam1, eps);
+    lam2 = entropy_fix(lam2, eps);
+    lam3 = entropy_fix(lam3, eps);
+    T sm = max4(fabs(lam1), fabs(lam2), fabs(lam3), fabs(lam3));
+    sMax = sm;
+
+    T s1 = T(0.5) * (sm + sm);
+    T s2 = T(0.5) * (sm - sm);
+    T qq = dsqrt(vel0 * vel0 + vel1 * vel1);
+    T G1 = gm1 * (((qq * qq) / T(2)) * dRho - (vel0 * dRV0 + vel1 * dRV1) + dRhoE);
+    T G2 = -u * dRho + (dRV0 * nx + dRV1 * ny);
+    T C1 = (G1 / (a * a)) * (s1 - sm) + G2 / a * s2;
+    T C2 = (G1 / a) * s2 + (s1 - sm) * G2;
+
+    T fL[4], fR[4];
+    convective_flux(pL, uL, vL, rhoL, qL[3], nx, ny, fL);
+    convective_flux(pR, uR, vR, rhoR, qR[3], nx, ny, fR);
+    T D0 = sm * dRho + C1;
+    T D1 = sm * dRV0 + C1 * vel0 + C2 * nx;
+    T D2 = sm * dRV1 + C1 * vel1 + C2 * ny;
+    T D3 = sm * dRhoE + C1 * h + C2 * u;
+    out[0] = T(0.5) * (fL[0] + fR[0]) - T(0.5) * D0;
+    out[1] = T(0.5) * (fL[1] + fR[1]) - T(0.5) * D1;
+    out[2] = T(0.5) * (fL[2] + fR[2]) - T(0.5) * D2;
+    out[3] = T(0.5) * (fL[3] + fR[3]) - T(0.5) * D3;
+}
+
+template <typename T>
+__device__ __forceinline__ void inviscid_flux(int kind, const T qL[4], const T qR[4], T nx, T ny, T out[4], T &sMax)
+{
+    if (kind == 1)
+        roe_flux(qL, qR, nx, ny, out, sMax);
+    else
+        rusanov_flux(qL, qR, nx, ny, out, sMax);
+}
+
+// source/flux.d:28-64.  dq[k][r] is d(q_k)/d(x_r).  The four 4x4 matrices are
+// scaled by mu/rho and applied row by row; structurally zero entries are skipped
+// (their products are signed zeros, which leave every non-zero sum unchanged).
+template <typename T>
+__device__ __forceinline__ void diffusive_flux(T Pr, T mu, const T q[4], const T dq[4][2], T nx, T ny, T out[4])
+{
+    T rho = q[0];
+    T u = q[1] / q[0];
+    T v = q[2] / q[0];
+    T E = q[3] / q[0];
+    T gP = K<T>::g / Pr;
+    T s = mu / rho;
+    const T c43 = T(-4.0 / 3.0), p43 = T(4.0 / 3.0), p23 = T(2.0 / 3.0), m23 = T(-2.0 / 3.0), c231 = T(2.0 / 3.0 - 1.0);
+    T tmp0 = (c43 + gP) * (u * u) + (T(-1.0) + gP) * (v * v) - gP * E;
+    T tmp1 = (T(-1.0) + gP) * (u * u) + (c43 + gP) * (v * v) - gP * E;
+    // A00 rows (row 0 is zero)
+    T a10 = s * (c43 * u), a11 = s * p43;
+    T a20 = s * (-v), a22 = s * T(1);
+    T a30 = s * tmp0, a31 = s * ((p43 - gP) * u), a32 = s * ((T(1.0) - gP) * v), a33 = s * gP;
+    // A01
+    T b10 = s * (p23 * v), b12 = s * m23;
+    T b20 = s * (-u), b21 = s * T(1);
+    T b30 = s * (c231 * u * v), b31 = s * v, b32 = s * (m23 * u);
+    // A10
+    T c10 = s * (-v), c12 = s * T(1);
+    T c20 = s * (p23 * u), c22 = s * m23;
+    T c30 = s * (c231 * u * v), c31 = s * (m23 * v), c32 = s * u;
+    // A11
+    T d10 = s * (-u), d11 = s * T(1);
+    T d20 = s * (c43 * v), d22 = s * p43;
+    T d30 = s * tmp1, d31 = s * ((T(1.0) - gP) * u), d32 = s * ((p43 - gP) * v), d33 = s * gP;
+    const T x0 = dq[0][0], x1 = dq[1][0], x2 = dq[2][0], x3 = dq[3][0];
+    const T y0 = dq[0][1], y1 = dq[1][1], y2 = dq[2][1], y3 = dq[3][1];
+    // matrix-vector products accumulate left to right from 0 (numd Matrix * Vector)
+    T G0_1 = (T(0.0) + a10 * x0 + a11 * x1) + (T(0.0) + b10 * y0 + b12 * y2);
+    T G0_2 = (T(0.0) + a20 * x0 + a22 * x2) + (T(0.0) + b20 * y0 + b21 * y1);
+    T G0_3 = (T(0.0) + a30 * x0 + a31 * x1 + a32 * x2 + a33 * x3) + (T(0.0) + b30 * y0 + b31 * y1 + b32 * y2);
+    T G1_1 = (T(0.0) + c10 * x0 + c12 * x2) + (T(0.0) + d10 * y0 + d11 * y1);
+    T G1_2 = (T(0.0) + c20 * x0 + c22 * x2) + (T(0.0) + d20 * y0 + d22 * y2);
+    T G1_3 = (T(0.0) + c30 * x0 + c31 * x1 + c32 * x2) + (T(0.0) + d30 * y0 + d31 * y1 + d32 * y2 + d33 * y3);
+    out[0] = T(0.0) * nx + T(0.0) * ny;
+    out[1] = G0_1 * nx + G1_1 * ny;
+    out[2] = G0_2 * nx + G1_2 * ny;
+    out[3] = G0_3 * nx + G1_3 * ny;
+}
+
+}  // namespace ebbdev

@@ -1,0 +1,175 @@
+// host_io.cpp -- .esln v2 solution files (source/io.d:55-161 saveSolution,
+// source/io.d:218-366 loadSolution), big-endian.
+//
+// Layout: u32 magic 0xEA98E1F5, u32 version (2), u32 cells, f64 t, f64 dt, u32 M (4),
+// u32 order; per cell in reference order: u32 global id, u8 edge count, 4 f64 state,
+// edge count x 4 f64 face states; then 4 CRC-32 bytes.  The reference computes the
+// CRC over its whole buffer including the 4 not-yet-written trailing bytes; this
+// writer takes those bytes as zero (what a freshly mapped buffer holds).  Readers,
+// the reference's included, do not check the CRC.
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "solver_impl.hpp"
+
+namespace {
+
+uint32_t crc_table[256];
+bool crc_init = false;
+
+void init_crc()
+{
+    for (uint32_t i = 0; i < 256; i++) {
+        uint32_t c = i;
+        for (int k = 0; k < 8; k++) c = (c & 1) ? (0xEDB88320u ^ (c >> 1)) : (c >> 1);
+        crc_table[i] = c;
+    }
+    crc_init = true;
+}
+
+uint32_t crc32(const uint8_t *p, size_t n)
+{
+    if (!crc_init) init_crc();
+    uint32_t c = 0xFFFFFFFFu;
+    for (size_t i = 0; i < n; i++) c = crc_table[(c ^ p[i]) & 0xff] ^ (c >> 8);
+    return c ^ 0xFFFFFFFFu;
+}
+
+struct BE {
+    std::vector<uint8_t> b;
+    void u32(uint32_t v)
+    {
+        for (int k = 3; k >= 0; k--) b.push_back((uint8_t)(v >> (8 * k)));
+    }
+    void u8(uint8_t v) { b.push_back(v); }
+    void f64(double d)
+    {
+        uint64_t v;
+        std::memcpy(&v, &d, 8);
+        for (int k = 7; k >= 0; k--) b.push_back((uint8_t)(v >> (8 * k)));
+    }
+};
+
+struct RD {
+    const uint8_t *p, *end;
+    bool ok = true;
+    uint32_t u32()
+    {
+        if (end - p < 4) {
+            ok = false;
+            return 0;
+        }
+        uint32_t v = ((uint32_t)p[0] << 24) | ((uint32_t)p[1] << 16) | ((uint32_t)p[2] << 8) | p[3];
+        p += 4;
+        return v;
+    }
+    uint8_t u8()
+    {
+        if (end - p < 1) {
+            ok = false;
+            return 0;
+        }
+        return *p++;
+    }
+    double f64()
+    {
+        if (end - p < 8) {
+            ok = false;
+            return 0;
+        }
+        uint64_t v = 0;
+        for (int k = 0; k < 8; k++) v = (v << 8) | p[k];
+        p += 8;
+        double d;
+        std::memcpy(&d, &v, 8);
+        return d;
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+int ebb_save_solution(ebb_solver *s, const char *path)
+{
+    if (!s || !path) return EBB_ERR_ARG;
+    const int64_t C = s->C;
+    std::vector<double> q(4 * C), f(4 * s->ref_face_slot.size());
+    int r = ebb_get_state(s, q.data());
+    if (r) return r;
+    if ((r = ebb_get_face_states(s, f.data()))) return r;
+    double t, dt;
+    int64_t it;
+    if ((r = ebb_get_time(s, &t, &dt, &it))) return r;
+    BE w;
+    w.b.reserve(40 + C * (5 + 32) + f.size() * 8);
+    w.u32(0xEA98E1F5u);
+    w.u32(2);
+    w.u32((uint32_t)C);
+    w.f64(t);
+    w.f64(dt);
+    w.u32(4);
+    w.u32((uint32_t)s->cfg.order);
+    size_t fo = 0;
+    for (int64_t i = 0; i < C; i++) {
+        w.u32((uint32_t)i);
+        const int ne = s->ref_nedge[i];
+        w.u8((uint8_t)ne);
+        for (int k = 0; k < 4; k++) w.f64(q[4 * i + k]);
+        for (int j = 0; j < ne; j++, fo++)
+            for (int k = 0; k < 4; k++) w.f64(f[4 * fo + k]);
+    }
+    const size_t body = w.b.size();
+    w.b.resize(body + 4, 0);
+    uint32_t c = crc32(w.b.data(), w.b.size());
+    w.b.resize(body);
+    for (int k = 0; k < 4; k++) w.u8((uint8_t)(c >> (8 * k)));
+    FILE *fp = std::fopen(path, "wb");
+    if (!fp) return EBB_ERR_IO;
+    size_t n = std::fwrite(w.b.data(), 1, w.b.size(), fp);
+    std::fclose(fp);
+    return n == w.b.size() ? EBB_OK : EBB_ERR_IO;
+}
+
+int ebb_load_solution(ebb_solver *s, const char *path)
+{
+    if (!s || !path) return EBB_ERR_ARG;
+    FILE *fp = std::fopen(path, "rb");
+    if (!fp) return EBB_ERR_IO;
+    std::vector<uint8_t> buf;
+    uint8_t tmp[1 << 16];
+    size_t n;
+    while ((n = std::fread(tmp, 1, sizeof tmp, fp)) > 0) buf.insert(buf.end(), tmp, tmp + n);
+    std::fclose(fp);
+    RD r{buf.data(), buf.data() + buf.size()};
+    if (r.u32() != 0xEA98E1F5u || !r.ok) return EBB_ERR_FORMAT;
+    uint32_t ver = r.u32();
+    uint32_t cells = r.u32();
+    if (!r.ok || cells != (uint32_t)s->C) return EBB_ERR_FORMAT;
+    double t = r.f64(), dt = r.f64();
+    std::vector<double> q(4 * s->C);
+    if (ver == 1) {
+        for (int64_t i = 0; i < s->C; i++)
+            for (int k = 0; k < 4; k++) q[4 * i + k] = r.f64();
+    } else if (ver == 2) {
+        uint32_t M = r.u32();
+        (void)r.u32();
+        if (M != 4) return EBB_ERR_FORMAT;
+        for (int64_t i = 0; i < s->C; i++) {
+            (void)r.u32();
+            int ne = r.u8();
+            for (int k = 0; k < 4; k++) q[4 * i + k] = r.f64();
+            for (int j = 0; j < ne; j++)
+                for (int k = 0; k < 4; k++) (void)r.f64();  // face states are recomputed by the next residual
+        }
+    } else {
+        return EBB_ERR_FORMAT;
+    }
+    if (!r.ok) return EBB_ERR_FORMAT;
+    int rc = ebb_set_state(s, q.data());
+    if (rc) return rc;
+    return ebb_set_time(s, t, dt);
+}
+
+}  // extern "C"

@@ -1,0 +1,40 @@
+// solver_impl.hpp -- the solver handle behind the C ABI (host side).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "host.hpp"
+#include "layout.h"
+
+struct ebb_solver {
+    ebb_config cfg;
+    int32_t precision = EBB_PREC_FP64;
+    int64_t C = 0, G = 0, Eint = 0, Cs = 0;
+    int32_t maxJ = 0;
+    double mu = 0;
+    std::vector<int32_t> perm;           // device cell -> reference cell
+    std::vector<int64_t> ref_face_slot;  // reference (cell, local edge) order -> device slot index
+    std::vector<int32_t> ref_nedge;      // edge count per reference cell
+    cudaStream_t stream = nullptr;
+    void *dmem = nullptr;
+    size_t dbytes = 0;
+    DMesh M{};
+    DPhys P{};
+    DArrays A{};
+    int32_t *d_perm = nullptr;
+    double *d_stage = nullptr;  // C x 4 doubles in reference order
+    int nred = 0;
+    cudaGraphExec_t g1 = nullptr, g16 = nullptr;  // 1-step and 16-step time-loop graphs
+    int32_t err_kind = 0;
+    int64_t err_index = -1;
+    std::string err_msg;
+};
+
+namespace ebb {
+int solver_sync_state(ebb_solver *s, DState &hst);
+int solver_write_state(ebb_solver *s, const DState &hst);
+int solver_run_residual_on_qs(ebb_solver *s, int limit, int dt_update, double *new_dt, double *rmax);
+}  // namespace ebb

@@ -1,0 +1,362 @@
+"""Seeded synthetic meshes for the benchmark workloads, written as gmsh 2.2 ASCII or
+handed over as arrays.
+
+The reference ships no generator (its meshes come from gmsh, not installed here).
+These follow the reader's constraints (source/io.d:689-990): sequential node and
+element numbers, line elements (type 1) carrying the physical tag as the first tag,
+tags 1..N in PhysicalNames order, triangles type 2, quads type 3.
+
+* ``wedge``: [0,3]x[0,1] minus the 15-degree ramp from x=0.5; triangles from a
+  seeded Delaunay triangulation of jittered points whose spacing is graded 2x finer
+  toward the ramp.  Tags: Inflow (x=0), Top (y=1), Symmetry (y=0, x<0.5), Ramp,
+  Outflow (x=3).
+* ``bump_channel``: [0,3]x[0,1] with a bump y = h sin^2(pi (x-1)) on 1<=x<=2;
+  Delaunay triangles.  Tags: Inflow, Outflow, Wall.
+* ``flat_plate``: [-0.5,2]x[0,0.5]; anisotropic quads in a wall layer (first cell
+  1e-4, growth 1.05) and Delaunay triangles above.  Tags: Inflow, Top, Outflow,
+  Symmetry (y=0, x<0), Wall (y=0, x>=0).
+* ``uniform_quads``: n x n quads on [0,1]^2 with one tag (Freestream).
+"""
+import math
+
+import numpy as np
+from scipy.spatial import Delaunay
+
+
+class MeshArrays:
+    def __init__(self, nodes, elements, b_nodes, b_group_start, tags):
+        self.nodes = np.asarray(nodes, dtype=np.float64)
+        self.elements = elements  # (M,3) / (M,4) int arrays (1-based) or list of lists
+        self.b_nodes = np.asarray(b_nodes, dtype=np.int64).reshape(-1, 2)
+        self.b_group_start = list(b_group_start)
+        self.tags = list(tags)
+
+    @property
+    def n_cells(self):
+        return sum(len(e) for e in self.elements) if isinstance(self.elements, list) else len(self.elements)
+
+    def element_list(self):
+        if isinstance(self.elements, list):
+            out = []
+            for e in self.elements:
+                out.extend(np.asarray(e).tolist())
+            return out
+        return self.elements.tolist()
+
+    def as_reader_dict(self):
+        """The dict shape the oracle's gmsh restatement returns."""
+        return {"nodes": self.nodes, "elements": self.element_list(), "bNodes": self.b_nodes,
+                "bGroupStart": self.b_group_start, "bTags": self.tags}
+
+    def to_solver_mesh(self):
+        from .solver import Mesh
+        els = self.elements
+        if isinstance(els, list):
+            blocks = [np.asarray(e, dtype=np.int64) for e in els if len(e)]
+            if len(blocks) == 1:
+                els = blocks[0]
+            else:
+                els = [r for b in blocks for r in b.tolist()]
+        return Mesh.from_arrays(self.nodes, els, self.b_nodes, self.b_group_start, self.tags)
+
+    def write_gmsh(self, path):
+        """gmsh 2.2 ASCII: line elements first (grouped by tag), then triangles/quads."""
+        tags = self.tags
+        ng = len(tags)
+        starts = list(self.b_group_start) + [len(self.b_nodes)]
+        with open(path, "w") as f:
+            f.write("$MeshFormat\n2.2 0 8\n$EndMeshFormat\n$PhysicalNames\n%d\n" % (ng + 1))
+            for i, t in enumerate(tags):
+                f.write('1 %d "%s"\n' % (i + 1, t))
+            f.write('2 %d "Flow"\n$EndPhysicalNames\n$Nodes\n%d\n' % (ng + 1, len(self.nodes)))
+            idx = np.arange(1, len(self.nodes) + 1)
+            np.savetxt(f, np.column_stack([idx, self.nodes[:, 0], self.nodes[:, 1], np.zeros(len(idx))]),
+                       fmt=["%d", "%.17g", "%.17g", "%d"])
+            blocks = self.elements if isinstance(self.elements, list) else [self.elements]
+            nel = len(self.b_nodes) + sum(len(b) for b in blocks)
+            f.write("$EndNodes\n$Elements\n%d\n" % nel)
+            k = 1
+            for g in range(ng):
+                bn = self.b_nodes[starts[g]:starts[g + 1]] + 1
+                n = len(bn)
+                ids = np.arange(k, k + n)
+                np.savetxt(f, np.column_stack([ids, np.ones(n, int), np.full(n, 2), np.full(n, g + 1),
+                                               np.full(n, g + 1), bn]), fmt="%d")
+                k += n
+            for b in blocks:
+                b = np.asarray(b, dtype=np.int64)
+                if len(b) == 0:
+                    continue
+                n = len(b)
+                typ = 2 if b.shape[1] == 3 else 3
+                ids = np.arange(k, k + n)
+                np.savetxt(f, np.column_stack([ids, np.full(n, typ), np.full(n, 2), np.full(n, ng + 1),
+                                               np.full(n, ng + 1), b]), fmt="%d")
+                k += n
+            f.write("$EndElements\n")
+
+
+def _boundary_groups(tri_nodes_xy, simplices, classify, tags):
+    """Boundary edges of a triangulation (edges used once), grouped by classify(midx, midy) -> tag index."""
+    e = np.concatenate([simplices[:, [0, 1]], simplices[:, [1, 2]], simplices[:, [2, 0]]])
+    es = np.sort(e, axis=1)
+    key = es[:, 0].astype(np.int64) * (len(tri_nodes_xy) + 1) + es[:, 1]
+    uniq, inv, cnt = np.unique(key, return_inverse=True, return_counts=True)
+    once = cnt[inv] == 1
+    be = e[once]
+    mid = 0.5 * (tri_nodes_xy[be[:, 0]] + tri_nodes_xy[be[:, 1]])
+    g = classify(mid[:, 0], mid[:, 1])
+    order = np.argsort(g, kind="stable")
+    be, g = be[order], g[order]
+    starts = [int(np.searchsorted(g, k)) for k in range(len(tags))]
+    return be, starts
+
+
+def _ccw(nodes, tris):
+    x, y = nodes[:, 0], nodes[:, 1]
+    a = (x[tris[:, 1]] - x[tris[:, 0]]) * (y[tris[:, 2]] - y[tris[:, 0]]) - \
+        (x[tris[:, 2]] - x[tris[:, 0]]) * (y[tris[:, 1]] - y[tris[:, 0]])
+    t = tris.copy()
+    t[a < 0] = t[a < 0][:, [0, 2, 1]]
+    return t, np.abs(a)
+
+
+def _polyline(points, h_fn, closed=False):
+    """Points along a polyline at local spacing h_fn(x, y)."""
+    out = []
+    pts = list(points) + ([points[0]] if closed else [])
+    for a, b in zip(pts[:-1], pts[1:]):
+        a, b = np.asarray(a, float), np.asarray(b, float)
+        L = np.linalg.norm(b - a)
+        s = 0.0
+        seg = [a]
+        while True:
+            p = a + (b - a) * (s / L)
+            s += h_fn(p[0], p[1])
+            if s >= L - 0.3 * h_fn(b[0], b[1]):
+                break
+            seg.append(a + (b - a) * (s / L))
+        out.extend(seg)
+    if not closed:
+        out.append(np.asarray(pts[-1], float))
+    return np.array(out)
+
+
+def _interior_points(rng, xlo, xhi, ylo, yhi, h_fn, inside, h0):
+    """Jittered points with local spacing ~ h_fn: a fine jittered grid thinned by
+    acceptance probability (h0/h)^2, keeping a minimum distance from the boundary."""
+    nx = int(math.ceil((xhi - xlo) / h0))
+    ny = int(math.ceil((yhi - ylo) / h0))
+    gx, gy = np.meshgrid((np.arange(nx) + 0.5) * h0 + xlo, (np.arange(ny) + 0.5) * h0 + ylo)
+    x = gx.ravel() + rng.uniform(-0.35, 0.35, gx.size) * h0
+    y = gy.ravel() + rng.uniform(-0.35, 0.35, gy.size) * h0
+    h = h_fn(x, y)
+    keep = rng.uniform(0, 1, x.size) < (h0 / h) ** 2
+    x, y = x[keep], y[keep]
+    m = inside(x, y, 0.5 * h_fn(x, y))
+    return np.column_stack([x[m], y[m]])
+
+
+def wedge(n_cells=1_000_000, seed=0, angle_deg=15.0, ramp_x=0.5):
+    rng = np.random.default_rng(seed)
+    ta = math.tan(math.radians(angle_deg))
+    ymax_ramp = (3.0 - ramp_x) * ta
+
+    def floor_y(x):
+        return np.where(x > ramp_x, (x - ramp_x) * ta, 0.0)
+
+    def dist_ramp(x, y):
+        return np.hypot(np.maximum(x - 3.0, 0) + np.minimum(x - ramp_x, 0), 0) * 0 + np.abs(y - floor_y(x))
+
+    # spacing graded 2x: h = hc near the floor/ramp (distance 0) to 2 hc at distance >= 0.5
+    area = 3.0 - 0.5 * (3.0 - ramp_x) * ymax_ramp
+    # triangles ~ 2 * points; mean (1/h^2) over the domain sets hc
+    def inv_h2_mean(hc):
+        xs = np.linspace(0, 3, 200)
+        tot = 0.0
+        for xv in xs:
+            yl = float(floor_y(np.array([xv]))[0])
+            ys = np.linspace(yl, 1, 100)
+            d = ys - yl
+            h = hc * (1 + np.clip(d / 0.5, 0, 1))
+            tot += np.mean(1 / h ** 2) * (1 - yl)
+        return tot / len(xs) * 3.0
+    hc = math.sqrt(inv_h2_mean(1.0) / (n_cells / 2.0))
+
+    def h_fn(x, y):
+        d = np.abs(np.asarray(y) - floor_y(np.asarray(x)))
+        return hc * (1 + np.clip(d / 0.5, 0, 1))
+
+    corners = [(0.0, 0.0), (ramp_x, 0.0), (3.0, ymax_ramp), (3.0, 1.0), (0.0, 1.0)]
+    bpts = _polyline(corners, lambda x, y: float(h_fn(np.array([x]), np.array([y]))[0]), closed=True)
+
+    def inside(x, y, margin):
+        return (x > margin) & (x < 3.0 - margin) & (y < 1.0 - margin) & (y - floor_y(x) > margin * 1.05)
+
+    ip = _interior_points(rng, 0.0, 3.0, 0.0, 1.0, h_fn, inside, hc)
+    nodes = np.vstack([bpts, ip])
+    tri = Delaunay(nodes).simplices.astype(np.int64)
+    tris, a = _ccw(nodes, tri)
+    tris = tris[a > 1e-14]
+    tags = ["Inflow", "Top", "Symmetry", "Ramp", "Outflow"]
+    eps = 1e-9
+
+    def classify(mx, my):
+        g = np.full(mx.shape, 1)
+        g[mx < eps] = 0
+        g[mx > 3.0 - eps] = 4
+        g[(my < eps) & (mx < ramp_x)] = 2
+        g[(mx >= ramp_x) & (np.abs(my - floor_y(mx)) < 1e-7) & (mx < 3.0 - eps)] = 3
+        return g
+
+    be, starts = _boundary_groups(nodes, tris, classify, tags)
+    return MeshArrays(nodes, tris + 1, be, starts, tags)
+
+
+def bump_channel(n_cells=20000, h=0.05, seed=0):
+    rng = np.random.default_rng(seed)
+
+    def floor_y(x):
+        x = np.asarray(x, float)
+        return np.where((x >= 1) & (x <= 2), h * np.sin(np.pi * (x - 1)) ** 2, 0.0)
+
+    area = 3.0 - 0.5 * h
+    hc = math.sqrt(area / (n_cells / 2.0))
+    hfun = lambda x, y: np.full(np.shape(x), hc) if np.ndim(x) else hc
+    xs = np.arange(0, 3 + 1e-12, hc)
+    xs[-1] = 3.0
+    bottom = np.column_stack([xs, floor_y(xs)])
+    top = np.column_stack([xs[::-1], np.ones_like(xs)])
+    ys = np.arange(hc, 1 - 0.5 * hc, hc)
+    right = np.column_stack([np.full_like(ys, 3.0), ys])
+    left = np.column_stack([np.zeros_like(ys), ys[::-1]])
+    bpts = np.vstack([bottom, right, top, left])
+
+    def inside(x, y, margin):
+        return (x > margin) & (x < 3 - margin) & (y < 1 - margin) & (y - floor_y(x) > margin)
+
+    ip = _interior_points(rng, 0, 3, 0, 1, lambda x, y: np.full(np.shape(x), hc), inside, hc)
+    nodes = np.vstack([bpts, ip])
+    tri = Delaunay(nodes).simplices.astype(np.int64)
+    tris, a = _ccw(nodes, tri)
+    tris = tris[a > 1e-14]
+    tags = ["Inflow", "Outflow", "Wall"]
+    eps = 1e-9
+
+    def classify(mx, my):
+        g = np.full(mx.shape, 2)
+        g[mx < eps] = 0
+        g[mx > 3 - eps] = 1
+        return g
+
+    be, starts = _boundary_groups(nodes, tris, classify, tags)
+    return MeshArrays(nodes, tris + 1, be, starts, tags)
+
+
+def flat_plate(n_cells=4_000_000, h1=1e-4, growth=1.05, seed=0, layer_top=None):
+    rng = np.random.default_rng(seed)
+    x0, x1, y1 = -0.5, 2.0, 0.5
+    # wall-layer column count sized so quads are ~12% of the cells
+    nl = 0
+    ys = [0.0]
+    hh = h1
+    while True:
+        ys.append(ys[-1] + hh)
+        hh *= growth
+        nl += 1
+        if (layer_top and ys[-1] >= layer_top) or (not layer_top and hh > 2.5e-3):
+            break
+    ys = np.array(ys)
+    H = ys[-1]
+    # tri region spacing graded from dx at the layer top to 4 dx at y1
+    def tri_count(dx):
+        yy = np.linspace(H, y1, 400)
+        h = dx * (1 + 3 * (yy - H) / (y1 - H))
+        return 2 * np.trapezoid((x1 - x0) / h ** 2, yy)
+    lo, hi = 1e-5, 1e-1
+    for _ in range(60):
+        dx = math.sqrt(lo * hi)
+        nc = tri_count(dx) + (x1 - x0) / dx * nl
+        if nc > n_cells:
+            lo = dx
+        else:
+            hi = dx
+    dx = math.sqrt(lo * hi)
+    nx = int(round((x1 - x0) / dx))
+    xs = np.linspace(x0, x1, nx + 1)
+    if not np.any(np.isclose(xs, 0.0)):
+        xs = np.sort(np.append(xs, 0.0))
+    X, Y = np.meshgrid(xs, ys)
+    qnodes = np.column_stack([X.ravel(), Y.ravel()])
+    ncol = len(xs)
+    qid = np.arange(len(qnodes)).reshape(len(ys), ncol)
+    quads = np.column_stack([qid[:-1, :-1].ravel(), qid[:-1, 1:].ravel(), qid[1:, 1:].ravel(), qid[1:, :-1].ravel()])
+
+    def h_fn(x, y):
+        return dx * (1 + 3 * np.clip((np.asarray(y) - H) / (y1 - H), 0, 1))
+
+    # triangle region boundary points: the layer top row is shared with the quads
+    top_row = qid[-1]
+    right = _polyline([(x1, H), (x1, y1)], lambda x, y: float(h_fn(x, y)))[1:]
+    topb = _polyline([(x1, y1), (x0, y1)], lambda x, y: float(h_fn(x, y)))[1:]
+    left = _polyline([(x0, y1), (x0, H)], lambda x, y: float(h_fn(x, y)))[1:-1]
+
+    def inside(x, y, margin):
+        return (x > x0 + margin) & (x < x1 - margin) & (y > H + margin) & (y < y1 - margin)
+
+    ip = _interior_points(rng, x0, x1, H, y1, h_fn, inside, dx)
+    tnodes_extra = np.vstack([right, topb, left, ip])
+    nodes = np.vstack([qnodes, tnodes_extra])
+    tri_set = np.concatenate([top_row, np.arange(len(qnodes), len(nodes))])
+    local = nodes[tri_set]
+    tri = Delaunay(local).simplices.astype(np.int64)
+    tri = tri_set[tri]
+    tris, a = _ccw(nodes, tri)
+    tris = tris[a > 1e-16]
+    # boundary: quads' left/right/bottom + triangles' outer edges
+    tags = ["Inflow", "Top", "Outflow", "Symmetry", "Wall"]
+    eps = 1e-12
+    bl = []
+    for j in range(ncol - 1):
+        a_, b_ = qid[0, j], qid[0, j + 1]
+        xm = 0.5 * (xs[j] + xs[j + 1])
+        bl.append((4 if xm >= 0 else 3, b_, a_))
+    for i in range(len(ys) - 1):
+        bl.append((0, qid[i + 1, 0], qid[i, 0]))
+        bl.append((2, qid[i, -1], qid[i + 1, -1]))
+
+    def classify(mx, my):
+        g = np.full(mx.shape, 1)
+        g[mx < x0 + eps] = 0
+        g[mx > x1 - eps] = 2
+        return g
+
+    tbe, tstarts = _boundary_groups(nodes, tris, classify, tags)
+    # drop the layer-top edges (shared with quads, not boundary)
+    mid_y = 0.5 * (nodes[tbe[:, 0], 1] + nodes[tbe[:, 1], 1])
+    keep = mid_y > H + 1e-12
+    tg = classify(0.5 * (nodes[tbe[:, 0], 0] + nodes[tbe[:, 1], 0]), mid_y)
+    allb = [(int(g), int(a_), int(b_)) for g, (a_, b_) in zip(tg[keep], tbe[keep])] + bl
+    allb.sort(key=lambda r: r[0])
+    g = np.array([r[0] for r in allb])
+    be = np.array([[r[1], r[2]] for r in allb], dtype=np.int64)
+    starts = [int(np.searchsorted(g, k)) for k in range(len(tags))]
+    return MeshArrays(nodes, [quads + 1, tris + 1], be, starts, tags)
+
+
+def uniform_quads(n=32):
+    xs = np.linspace(0, 1, n + 1)
+    X, Y = np.meshgrid(xs, xs)
+    nodes = np.column_stack([X.ravel(), Y.ravel()])
+    qid = np.arange(len(nodes)).reshape(n + 1, n + 1)
+    quads = np.column_stack([qid[:-1, :-1].ravel(), qid[:-1, 1:].ravel(), qid[1:, 1:].ravel(), qid[1:, :-1].ravel()])
+    b = []
+    for j in range(n):
+        b.append((qid[0, j], qid[0, j + 1]))
+    for i in range(n):
+        b.append((qid[i, n], qid[i + 1, n]))
+    for j in range(n, 0, -1):
+        b.append((qid[n, j], qid[n, j - 1]))
+    for i in range(n, 0, -1):
+        b.append((qid[i, 0], qid[i - 1, 0]))
+    return MeshArrays(nodes, quads + 1, np.array(b), [0], ["Freestream"])

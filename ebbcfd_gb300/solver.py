@@ -1,0 +1,283 @@
+"""Python face of the GB300 solver, mirroring the reference's operator interface.
+
+Names follow EbbCFD's D modules:
+  load_config            source/config.d:112 loadConfig
+  import_mesh            source/io.d:669 importMesh
+  UfvmSolver.ufvm_solver source/solve.d:322 ufvmSolver!(F,4)(R, q, mesh, config, newDt, Rmax, limit, dtUpdate)
+  UfvmSolver.step        source/integrators.d Euler/RK2/RK2_TVD/RK4 .step!solver
+  UfvmSolver.run         app/solver.d:38 runIntegrator loop body
+  roe_flux / rusanov_flux  source/flux.d:224 / :66
+  save_solution / load_solution  source/io.d:68 / :218
+
+Every call goes through the C ABI of include/ebb_gb300.h into the CUDA library; there
+is no CPU path.  Failures raise EbbError (EdgeException / CellException for the NaN
+checks the reference reports with those exception types).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+
+PRECISION = {"fp64": 0, "split": 1}
+FLUX = {"rusanovFlux": 0, "roeFlux": 1}
+INTEGRATOR = {"Euler": 0, "RK2": 1, "RK2_TVD": 2, "RK4": 3}
+BC = {"fullState": 0, "constP": 1, "inviscidWall": 2, "viscidWall": 3, "symmetry": 4, "tpInflow": 5, "dirichlet": 6}
+
+
+class EbbError(RuntimeError):
+    def __init__(self, code, msg, index=-1):
+        super().__init__("%s (%d): %s%s" % (_lib.STATUS.get(code, "?"), code, msg,
+                                            "" if index < 0 else " [index %d]" % index))
+        self.code = code
+        self.index = index
+
+
+class EdgeException(EbbError):
+    """NaN face flux (solve.d:805-806 and siblings); index is the reference edge id."""
+
+
+class CellException(EbbError):
+    """NaN cell state after a step (app/solver.d:131-149); index is the reference cell id."""
+
+
+def _check(code, msg="", index=-1):
+    if code == 0:
+        return
+    if code == 8:
+        raise EdgeException(code, msg or "Got NaN on edge", index)
+    if code == 9:
+        raise CellException(code, msg or "Got nan on cell average value", index)
+    raise EbbError(code, msg, index)
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def load_config(text):
+    """Parse ebb-solve JSON (config.d semantics) into the C config struct."""
+    L = _lib.load()
+    cfg = _lib.Config()
+    err = C.create_string_buffer(512)
+    _check(L.ebb_config_parse(text.encode(), C.byref(cfg), err, 512), err.value.decode())
+    return cfg
+
+
+def default_config():
+    cfg = _lib.Config()
+    _lib.load().ebb_config_defaults(C.byref(cfg))
+    return cfg
+
+
+def set_boundaries(cfg, bcs):
+    """bcs: list of (tag, type-name, [data...])."""
+    cfg.n_boundaries = len(bcs)
+    for i, (tag, typ, data) in enumerate(bcs):
+        b = cfg.boundaries[i]
+        b.tag = tag.encode()
+        b.type = BC[typ] if isinstance(typ, str) else int(typ)
+        b.n_data = len(data)
+        for k, v in enumerate(data):
+            b.data[k] = float(v)
+    return cfg
+
+
+def set_force_boundary(cfg, tags):
+    cfg.n_force = len(tags)
+    for i, t in enumerate(tags):
+        cfg.force_boundary[i].value = t.encode()
+    return cfg
+
+
+class Mesh:
+    """A gmsh mesh as the reference reads it (nodes, elements, boundary groups)."""
+
+    def __init__(self, handle):
+        self.h = handle
+        self._info = None
+
+    @classmethod
+    def from_arrays(cls, nodes, elements, b_nodes, b_group_start, tags):
+        """nodes (N,2); elements: list of 1-based node lists or (M,k) array; b_nodes (B,2) 0-based."""
+        L = _lib.load()
+        xy = np.ascontiguousarray(np.asarray(nodes, dtype=np.float64)[:, :2])
+        if isinstance(elements, np.ndarray) and elements.ndim == 2:
+            off = np.arange(0, elements.size + 1, elements.shape[1], dtype=np.int64)
+            en = np.ascontiguousarray(elements.reshape(-1), dtype=np.int32)
+        else:
+            lens = [len(e) for e in elements]
+            off = np.zeros(len(elements) + 1, dtype=np.int64)
+            off[1:] = np.cumsum(lens)
+            en = np.ascontiguousarray(np.concatenate([np.asarray(e, dtype=np.int32) for e in elements]))
+        bn = np.ascontiguousarray(np.asarray(b_nodes, dtype=np.int32).reshape(-1, 2))
+        bgs = np.ascontiguousarray(np.asarray(b_group_start, dtype=np.int64))
+        tb = b"".join(t.encode().ljust(_lib.TAG_LEN, b"\0")[:_lib.TAG_LEN] for t in tags)
+        h = C.c_void_p()
+        err = C.create_string_buffer(512)
+        code = L.ebb_mesh_from_arrays(len(xy), _dp(xy), len(off) - 1, off.ctypes.data_as(C.POINTER(C.c_int64)),
+                                      en.ctypes.data_as(C.POINTER(C.c_int32)), len(bn),
+                                      bn.ctypes.data_as(C.POINTER(C.c_int32)), len(tags),
+                                      bgs.ctypes.data_as(C.POINTER(C.c_int64)), tb, C.byref(h), err, 512)
+        _check(code, err.value.decode())
+        return cls(h)
+
+    @property
+    def info(self):
+        if self._info is None:
+            inf = _lib.MeshInfo()
+            _check(_lib.load().ebb_mesh_get_info(self.h, C.byref(inf)))
+            self._info = inf
+        return self._info
+
+    @property
+    def n_cells(self):
+        return self.info.n_cells
+
+    @property
+    def tags(self):
+        L = _lib.load()
+        out = []
+        for i in range(self.info.n_tags):
+            b = C.create_string_buffer(_lib.TAG_LEN)
+            L.ebb_mesh_get_tag(self.h, i, b, _lib.TAG_LEN)
+            out.append(b.value.decode())
+        return out
+
+    def centroids(self):
+        xy = np.zeros((self.n_cells, 2))
+        _check(_lib.load().ebb_mesh_centroids(self.h, _dp(xy)))
+        return xy
+
+    def __del__(self):
+        try:
+            if self.h:
+                _lib.load().ebb_mesh_free(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
+def import_mesh(path):
+    L = _lib.load()
+    h = C.c_void_p()
+    err = C.create_string_buffer(512)
+    _check(L.ebb_mesh_import(str(path).encode(), C.byref(h), err, 512), err.value.decode())
+    return Mesh(h)
+
+
+class UfvmSolver:
+    """Device-resident solver for one mesh + config (buildMesh + ufvmSetup)."""
+
+    def __init__(self, mesh, cfg, precision="fp64"):
+        L = _lib.load()
+        self.mesh = mesh
+        self.cfg = cfg
+        self.n_cells = mesh.n_cells
+        self.face_slots = mesh.info.face_slots
+        h = C.c_void_p()
+        err = C.create_string_buffer(512)
+        code = L.ebb_solver_create(mesh.h, C.byref(cfg), PRECISION[precision], C.byref(h), err, 512)
+        _check(code, err.value.decode())
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            _lib.load().ebb_solver_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _raise(self, code):
+        if code == 0:
+            return
+        L = _lib.load()
+        kind = C.c_int32()
+        idx = C.c_int64()
+        msg = C.create_string_buffer(256)
+        L.ebb_last_error(self.h, C.byref(kind), C.byref(idx), msg, 256)
+        _check(code, msg.value.decode(), idx.value)
+
+    @property
+    def state(self):
+        q = np.zeros((self.n_cells, 4))
+        self._raise(_lib.load().ebb_get_state(self.h, _dp(q)))
+        return q
+
+    def set_state(self, q):
+        q = np.ascontiguousarray(q, dtype=np.float64).reshape(self.n_cells, 4)
+        self._raise(_lib.load().ebb_set_state(self.h, _dp(q)))
+
+    def time(self):
+        t = C.c_double()
+        dt = C.c_double()
+        it = C.c_int64()
+        self._raise(_lib.load().ebb_get_time(self.h, C.byref(t), C.byref(dt), C.byref(it)))
+        return t.value, dt.value, it.value
+
+    def set_time(self, t, dt):
+        self._raise(_lib.load().ebb_set_time(self.h, float(t), float(dt)))
+
+    def ufvm_solver(self, q, limit=True, dt_update=True, rmax=0.0):
+        """One residual evaluation; returns (R, newDt, Rmax)."""
+        q = np.ascontiguousarray(q, dtype=np.float64).reshape(self.n_cells, 4)
+        R = np.zeros_like(q)
+        nd = C.c_double()
+        rm = C.c_double(rmax)
+        self._raise(_lib.load().ebb_residual(self.h, _dp(q), _dp(R), C.byref(nd), C.byref(rm), int(limit),
+                                             int(dt_update)))
+        return R, nd.value, rm.value
+
+    def step(self, dt, rmax=0.0):
+        """One integrator step on the resident state; returns (next dt, Rmax)."""
+        d = C.c_double(dt)
+        rm = C.c_double(rmax)
+        self._raise(_lib.load().ebb_step(self.h, C.byref(d), C.byref(rm)))
+        return d.value, rm.value
+
+    def run(self, nsteps, records=True):
+        """Up to nsteps runIntegrator iterations; returns an (n, 11) array of
+        (t, drag, lift, resid_rho, resid_u, resid_v, resid_E, Rmax, dt, cfl) rows + step count."""
+        L = _lib.load()
+        n = C.c_int64()
+        if records:
+            rec = (_lib.StepRecord * max(1, nsteps))()
+            self._raise(L.ebb_run(self.h, int(nsteps), rec, C.byref(n)))
+            arr = np.frombuffer(rec, dtype=np.float64).reshape(-1, 10)[:n.value].copy()
+            return arr
+        self._raise(L.ebb_run(self.h, int(nsteps), None, C.byref(n)))
+        return n.value
+
+    def face_states(self):
+        out = np.zeros((self.face_slots, 4))
+        self._raise(_lib.load().ebb_get_face_states(self.h, _dp(out)))
+        return out
+
+    def save_solution(self, path):
+        self._raise(_lib.load().ebb_save_solution(self.h, str(path).encode()))
+
+    def load_solution(self, path):
+        self._raise(_lib.load().ebb_load_solution(self.h, str(path).encode()))
+
+
+def _flux(kind, qL, qR, n):
+    L = _lib.load()
+    qL = np.ascontiguousarray(qL, dtype=np.float64).reshape(-1, 4)
+    qR = np.ascontiguousarray(qR, dtype=np.float64).reshape(-1, 4)
+    n = np.ascontiguousarray(n, dtype=np.float64).reshape(-1, 2)
+    F = np.zeros_like(qL)
+    s = np.zeros(len(qL))
+    _check(L.ebb_flux(kind, len(qL), _dp(qL), _dp(qR), _dp(n), _dp(F), _dp(s)))
+    return F, s
+
+
+def roe_flux(qL, qR, n):
+    return _flux(1, qL, qR, n)
+
+
+def rusanov_flux(qL, qR, n):
+    return _flux(0, qL, qR, n)

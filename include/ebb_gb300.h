@@ -1,0 +1,235 @@
+/*
+ * ebb_gb300.h -- C ABI of the GB300-native explicit unstructured finite-volume update.
+ *
+ * Every entry point is plain C: pointers, sizes and status codes, no C++ or torch
+ * types.  The caller owns host buffers; the library owns device memory.  A solver
+ * handle is bound to one CUDA stream and is not thread-safe; use one handle per
+ * host thread.  Calls never abort the process and kernels never trap: failures
+ * come back as an ebb_status, and ebb_last_error() gives the detail.
+ *
+ * Reference interfaces replaced (EbbCFD, D sources):
+ *   ebb_config_parse       source/config.d:112-313   loadConfig(string) -> Config
+ *   ebb_mesh_import        source/io.d:669-990       importMesh / parseGmshMesh (gmsh 2.2 ASCII)
+ *   ebb_solver_create      source/mesh.d:217-643     UMesh2.buildMesh
+ *                          source/solve.d:175-279    ufvmSetup (IC and BC binding)
+ *   ebb_residual           source/solve.d:322-1122   ufvmSolver!(F,4)(R, q, mesh, config, newDt, Rmax, limit, dtUpdate)
+ *   ebb_step               source/integrators.d:17-270  Euler/RK2/RK2_TVD/RK4.step!solver(R, q, mesh, config, dt, Rmax)
+ *   ebb_run                app/solver.d:38-277       runIntegrator loop body (NaN check, RMS, forces, CFL adjust, dt/t)
+ *   ebb_flux               source/flux.d:66-141,224-303  rusanovFlux!4 / roeFlux!4 (qL, qR, n, ref sMax)
+ *   ebb_save_solution      source/io.d:68-161        saveSolution (.esln v2, big-endian)
+ *   ebb_load_solution      source/io.d:218-366       loadSolution
+ */
+#ifndef EBB_GB300_H
+#define EBB_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EBB_ABI_VERSION 1
+#define EBB_MAX_BC 32
+#define EBB_MAX_FORCE_TAGS 8
+#define EBB_TAG_LEN 64
+#define EBB_PATH_LEN 1024
+
+typedef enum {
+    EBB_OK = 0,
+    EBB_ERR_ARG = 1,        /* bad argument or handle */
+    EBB_ERR_IO = 2,         /* file could not be opened/read/written */
+    EBB_ERR_FORMAT = 3,     /* malformed gmsh / JSON / .esln */
+    EBB_ERR_MESH = 4,       /* mesh topology/geometry rejected (e.g. non-positive area) */
+    EBB_ERR_CONFIG = 5,     /* config inconsistent with mesh (e.g. missing BC tag) */
+    EBB_ERR_CUDA = 6,       /* CUDA runtime failure */
+    EBB_ERR_OOM = 7,        /* device allocation failed */
+    EBB_ERR_NAN_EDGE = 8,   /* NaN face flux (reference: EdgeException, solve.d:806-1076) */
+    EBB_ERR_NAN_CELL = 9,   /* NaN cell state after a step (reference: CellException, app/solver.d:131-149) */
+    EBB_ERR_NO_DEVICE = 10, /* no CUDA device / extension not usable */
+    EBB_ERR_BC = 11,        /* boundary condition failed (tpInflow: both Mach roots negative, solve.d:662-669) */
+    EBB_ERR_LIMIT = 12      /* size beyond a documented limit */
+} ebb_status;
+
+/* boundary types, same order as enum BoundaryType (source/mesh.d:27-36) */
+typedef enum {
+    EBB_BC_FULL_STATE = 0,
+    EBB_BC_CONST_PRESSURE = 1,
+    EBB_BC_INVISCID_WALL = 2,
+    EBB_BC_VISCOUS_WALL = 3,
+    EBB_BC_SYMMETRY = 4,
+    EBB_BC_TEMP_PRES_INFLOW = 5,
+    EBB_BC_DIRICHLET = 6
+} ebb_bc_type;
+
+/* flux names of fluxList (source/flux.d:12) */
+typedef enum { EBB_FLUX_RUSANOV = 0, EBB_FLUX_ROE = 1 } ebb_flux_kind;
+/* integrator names of integratorList (source/integrators.d:17) */
+typedef enum { EBB_INT_EULER = 0, EBB_INT_RK2 = 1, EBB_INT_RK2_TVD = 2, EBB_INT_RK4 = 3 } ebb_integrator;
+
+/* precision forms */
+typedef enum {
+    EBB_PREC_FP64 = 0, /* plain FP64 path, same operation order as the reference */
+    EBB_PREC_SPLIT = 1 /* FP32 flux/gradient/limiter arithmetic, FP64 geometry, state update and reductions */
+} ebb_precision;
+
+/* manufactured-solution fields used by Dirichlet boundaries and the source term */
+typedef enum {
+    EBB_MMS_NONE = 0,
+    EBB_MMS_REFERENCE = 1, /* source/manufacturedsolution.d:27-282 */
+    EBB_MMS_SINE = 2       /* rho=1+0.1 sin(2pi x)cos(2pi y), u=0.5+0.05 cos(2pi x)sin(2pi y),
+                              v=0.3+0.05 sin(2pi x+1), p=1/1.4+0.1 cos(2pi y) (Euler source) */
+} ebb_mms;
+
+typedef struct {
+    char tag[EBB_TAG_LEN];
+    int32_t type;   /* ebb_bc_type */
+    int32_t n_data; /* entries of "q" */
+    double data[8];
+} ebb_boundary;
+
+/* struct Config (source/config.d:72-94), flattened. */
+typedef struct {
+    char mesh_file[EBB_PATH_LEN];
+    double dt;
+    int32_t dynamic_dt;
+    double t_end;
+    int32_t flux; /* ebb_flux_kind */
+    int64_t save_iter;
+    int64_t plot_iter;
+    int32_t n_force;
+    char force_boundary[EBB_MAX_FORCE_TAGS][EBB_TAG_LEN];
+    int32_t integrator; /* ebb_integrator */
+    int32_t limited;
+    double lp_thresh;
+    int64_t order;
+    double cfl;
+    double ic[4]; /* M, aoa (deg), p (unused), rho */
+    int32_t n_boundaries;
+    ebb_boundary boundaries[EBB_MAX_BC];
+    int32_t local_timestep;
+    int32_t multistage_limiting;
+    int32_t cfl_adjust;
+    int32_t viscosity;
+    double pr, r_gas, gamma, mu, re, l_ref; /* physicalConfig; gamma is parsed but 1.4 is used (euler.d:89) */
+    int32_t mms;                            /* ebb_mms; 0 for ebb-solve configs */
+} ebb_config;
+
+typedef struct ebb_mesh ebb_mesh;
+typedef struct ebb_solver ebb_solver;
+
+typedef struct {
+    int64_t n_nodes;
+    int64_t n_cells;      /* interior cells (elements) */
+    int64_t n_ghost;      /* boundary edges = ghost cells */
+    int64_t n_edges;      /* interior + boundary edges */
+    int64_t n_int_edges;
+    int32_t n_tags;
+    int32_t max_edges;    /* largest element edge count */
+    int64_t face_slots;   /* sum of element edge counts */
+} ebb_mesh_info;
+
+/* per-step record of ebb_run (the quantities app/solver.d:178-230 prints and writes) */
+typedef struct {
+    double t;      /* time before the increment (the .frc time column) */
+    double drag;   /* ld[0] */
+    double lift;   /* ld[1] */
+    double resid[4];
+    double rmax;   /* Flux_R */
+    double dt;     /* dt after the step's update */
+    double cfl;
+} ebb_step_record;
+
+/* ---- library ---------------------------------------------------------- */
+int ebb_abi_version(void);
+/* sizeof the public structs, for FFI bindings to check their layout */
+int ebb_struct_sizes(size_t *config, size_t *mesh_info, size_t *step_record);
+/* Returns EBB_OK when a CUDA device is usable (sets *n_devices). */
+int ebb_device_count(int *n_devices);
+/* Select the device later solver handles are created on (one GPU per process). */
+int ebb_set_device(int device);
+/* Page-locked host buffers for fast state copies (cudaMallocHost / cudaFreeHost). */
+int ebb_host_alloc(size_t bytes, void **ptr);
+int ebb_host_free(void *ptr);
+
+/* ---- config (source/config.d:112-313) ---------------------------------- */
+void ebb_config_defaults(ebb_config *cfg);
+int ebb_config_parse(const char *json_text, ebb_config *out, char *err, size_t err_len);
+
+/* ---- mesh (source/io.d:669-990) ---------------------------------------- */
+int ebb_mesh_import(const char *path, ebb_mesh **out, char *err, size_t err_len);
+/* Build from arrays: xy[2*n_nodes]; elem_off[n_elem+1]; elem_nodes 1-based node
+   numbers (any orientation; clockwise elements are reversed as io.d:969-987 does);
+   b_nodes[2*n_b] 0-based; b_group_start[n_tags]; tags as n_tags NUL-terminated strings
+   packed at stride EBB_TAG_LEN. */
+int ebb_mesh_from_arrays(int64_t n_nodes, const double *xy, int64_t n_elem, const int64_t *elem_off,
+                         const int32_t *elem_nodes, int64_t n_b, const int32_t *b_nodes, int32_t n_tags,
+                         const int64_t *b_group_start, const char *tags, ebb_mesh **out, char *err, size_t err_len);
+int ebb_mesh_get_info(const ebb_mesh *mesh, ebb_mesh_info *info);
+int ebb_mesh_get_tag(const ebb_mesh *mesh, int32_t i, char *tag, size_t len);
+/* element centroids in reference cell order (cx, cy), for initial conditions and error norms */
+int ebb_mesh_centroids(const ebb_mesh *mesh, double *xy);
+void ebb_mesh_free(ebb_mesh *mesh);
+
+/* ---- solver (buildMesh + ufvmSetup) ------------------------------------ */
+int ebb_solver_create(const ebb_mesh *mesh, const ebb_config *cfg, int32_t precision, ebb_solver **out, char *err,
+                      size_t err_len);
+void ebb_solver_destroy(ebb_solver *s);
+int ebb_last_error(const ebb_solver *s, int32_t *kind, int64_t *index, char *msg, size_t msg_len);
+
+/* state in reference cell order, q[n_cells][4] */
+int ebb_set_state(ebb_solver *s, const double *q);
+int ebb_get_state(ebb_solver *s, double *q);
+int ebb_get_time(ebb_solver *s, double *t, double *dt, int64_t *iterations);
+int ebb_set_time(ebb_solver *s, double t, double dt);
+
+/* One residual evaluation (ufvmSolver, plus the manufactured source when cfg.mms != 0)
+   on host state q[n_cells][4]; writes R[n_cells][4]; *new_dt is the CFL time step and
+   *rmax = max(*rmax, max|sum of len*flux|) as solve.d:1080-1121. */
+int ebb_residual(ebb_solver *s, const double *q, double *R, double *new_dt, double *rmax, int32_t limit,
+                 int32_t dt_update);
+/* Same on device buffers already laid out by the solver (q_dev/R_dev hold n_cells x 4
+   doubles in reference order); no host copies. */
+int ebb_residual_device(ebb_solver *s, const double *q_dev, double *R_dev, double *new_dt, double *rmax,
+                        int32_t limit, int32_t dt_update);
+
+/* One integrator step on the resident state with time step *dt; on return *dt is the
+   next step's CFL time step and *rmax the step's Flux_R (integrators.d). */
+int ebb_step(ebb_solver *s, double *dt, double *rmax);
+
+/* Up to max_steps iterations of the runIntegrator loop (stops at t >= tEnd).  Records
+   (may be NULL) receive one entry per step run; *steps_run the count. */
+int ebb_run(ebb_solver *s, int64_t max_steps, ebb_step_record *records, int64_t *steps_run);
+
+/* ebb_run without records, also returning the device time of the launched steps
+   measured with CUDA events on the solver's stream (no host synchronisation between
+   the events). */
+int ebb_run_timed(ebb_solver *s, int64_t max_steps, int64_t *steps_run, double *device_ms);
+
+/* Face states of the last residual evaluation per cell and local edge, reference order
+   (the edge values .esln v2 stores, io.d:111-133): out[face_slots][4]. */
+int ebb_get_face_states(ebb_solver *s, double *out);
+
+/* The CUDA stream (cudaStream_t) the solver launches on, for callers that time or
+   order work around it with CUDA events. */
+int ebb_get_stream(ebb_solver *s, void **stream);
+/* Average device time (ms, CUDA events on the solver stream) of each kernel of one
+   first-stage pass on the resident state, over n_rep launches each:
+   ms[0] cell (gradients, limiters, face states), ms[1] flux, ms[2] residual/update,
+   ms[3] step end.  The state is left as it was. */
+int ebb_profile_kernels(ebb_solver *s, int32_t n_rep, double *ms);
+
+/* ---- flux seam (source/flux.d) ------------------------------------------ */
+/* Batched device evaluation of rusanovFlux!4 / roeFlux!4 on host arrays:
+   qL,qR[n][4], normal[n][2] -> F[n][4], s_max[n]. */
+int ebb_flux(int32_t kind, int64_t n, const double *qL, const double *qR, const double *normal, double *F,
+             double *s_max);
+
+/* ---- files ---------------------------------------------------------------- */
+int ebb_save_solution(ebb_solver *s, const char *path);
+int ebb_load_solution(ebb_solver *s, const char *path);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,216 @@
+"""Host side of the C ABI without a GPU: library load and exports, config parsing
+(source/config.d:112-313 semantics), gmsh import (source/io.d:689-990 semantics)
+checked against the oracle's restatement, and loud failure of the compute entry
+points when no device is present."""
+import ctypes as C
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+import ebbcfd_gb300 as E
+from ebbcfd_gb300 import _lib, meshgen
+from oracle import gmsh_ref
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    text = open(os.path.join(ROOT, "include", "ebb_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(ebb_\w+)\s*\(", text)))
+
+
+def test_library_exports_every_header_symbol():
+    L = _lib.load()
+    names = header_functions()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(L, n), n
+        assert n in _lib.SIGNATURES, n
+    assert L.ebb_abi_version() == 1
+
+
+def test_struct_layout_matches_binding():
+    L = _lib.load()
+    a, b, c = C.c_size_t(), C.c_size_t(), C.c_size_t()
+    assert L.ebb_struct_sizes(C.byref(a), C.byref(b), C.byref(c)) == 0
+    assert a.value == C.sizeof(_lib.Config)
+    assert b.value == C.sizeof(_lib.MeshInfo)
+    assert c.value == C.sizeof(_lib.StepRecord)
+
+
+CONFIGS = sorted(f for f in glob.glob(os.path.join(ROOT, "tests", "golden", "meshes", "*.json"))
+                 if not f.endswith("manifest.json"))
+
+
+@pytest.mark.parametrize("path", CONFIGS, ids=[os.path.basename(p) for p in CONFIGS])
+def test_config_parse_matches_reference_semantics(path):
+    text = open(path).read()
+    cfg = E.load_config(text)
+    r = gmsh_ref.load_config(text)
+    assert cfg.mesh_file.decode() == r["mesh"]
+    assert cfg.flux == gmsh_ref.FLUXES[r["flux"]]
+    assert cfg.integrator == gmsh_ref.INTEGRATORS[r["integrator"]]
+    assert cfg.dt == r["dt"] and cfg.t_end == r["tEnd"] and cfg.cfl == r["CFL"]
+    assert cfg.save_iter == r["saveIter"] and cfg.plot_iter == r["plotIter"]
+    assert bool(cfg.limited) == r["limited"] and bool(cfg.dynamic_dt) == r["dynamicDt"]
+    assert bool(cfg.local_timestep) == r["localTimestep"] and bool(cfg.viscosity) == r["viscosity"]
+    assert bool(cfg.cfl_adjust) == r["cflAdjust"] and bool(cfg.multistage_limiting) == r["multistageLimiting"]
+    assert cfg.lp_thresh == r["lpThresh"] and cfg.order == r["order"]
+    assert list(cfg.ic) == r["ic"]
+    pc = r["physicalConfig"]
+    assert (cfg.pr, cfg.r_gas, cfg.re, cfg.l_ref) == (pc["Pr"], pc["R"], pc["Re"], pc["L"])
+    assert cfg.n_boundaries == len(r["boundaries"])
+    for i, b in enumerate(r["boundaries"]):
+        B = cfg.boundaries[i]
+        assert B.tag.decode() == b["tag"] and B.type == b["type"]
+        assert [B.data[k] for k in range(B.n_data)] == b["q"]
+    assert [cfg.force_boundary[k].value.decode() for k in range(cfg.n_force)] == r["forceBoundary"]
+
+
+BASE = """{"mesh": "m.msh", "dt": 0.001, "tEnd": 1, "flux": "roeFlux", "saveIter": -1, "plotIter": -1,
+ "forceBoundary": ["Wall", "Other"], "initialConditions": [0.5, 0, 1, 1],
+ "boudaryConditions": [{"tag": "Wall", "type": "madeUpType", "q": [0.5, 0, 1, 1]}] %s}"""
+
+
+def test_config_defaults_and_quirks():
+    c = E.load_config(BASE % "")
+    # absent keys take the reference defaults (config.d:137-260)
+    assert c.cfl == 0.5 and c.dynamic_dt == 1 and c.integrator == 0 and c.limited == 1
+    assert c.local_timestep == 0 and c.lp_thresh == -1 and c.order == 2 and c.multistage_limiting == 1
+    assert c.cfl_adjust == 1 and c.viscosity == 0 and (c.pr, c.r_gas, c.re, c.l_ref) == (0.7, 8.3145, 1000, 1)
+    # unknown boundary type keeps the enum default FullState (config.d:273-301)
+    assert c.boundaries[0].type == 0
+    assert c.n_force == 2
+    # present flags are true only when JSON true
+    c = E.load_config(BASE % ', "limited": 1, "dynamicDt": false, "order": 3, "CFL": 2')
+    assert c.limited == 0 and c.dynamic_dt == 0 and c.order == 2 and c.cfl == 2.0
+    # a partial physicalConfig falls back to all defaults
+    c = E.load_config(BASE % ', "physicalConfig": {"Pr": 0.9}')
+    assert c.pr == 0.7
+    # dt must be a floating-point literal (config.d:119 uses .floating)
+    with pytest.raises(E.EbbError):
+        E.load_config((BASE % "").replace('"dt": 0.001', '"dt": 1'))
+    with pytest.raises(E.EbbError):
+        E.load_config((BASE % "").replace('"roeFlux"', '"hllFlux"'))
+    with pytest.raises(E.EbbError):
+        E.load_config("{not json")
+    # single-string forceBoundary
+    c = E.load_config((BASE % "").replace('["Wall", "Other"]', '"Wall"'))
+    assert c.n_force == 1 and c.force_boundary[0].value == b"Wall"
+
+
+MESHES = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "meshes", "*.msh")))
+
+
+@pytest.mark.parametrize("path", MESHES, ids=[os.path.basename(p) for p in MESHES])
+def test_gmsh_import_matches_reference_reader(path):
+    m = E.import_mesh(path)
+    r = gmsh_ref.parse_gmsh(path)
+    assert m.n_cells == len(r["elements"])
+    assert m.tags == r["bTags"]
+    assert m.info.face_slots == sum(len(e) for e in r["elements"])
+    # centroids follow the CCW-corrected element orientation
+    xy = m.centroids()
+    for i in (0, len(xy) // 2, len(xy) - 1):
+        el = np.array(r["elements"][i]) - 1
+        p = r["nodes"][el]
+        assert np.allclose(xy[i], p.mean(axis=0), atol=0.5 * np.ptp(p, axis=0).max())
+
+
+def write(tmp_path, name, text):
+    p = tmp_path / name
+    p.write_text(text)
+    return str(p)
+
+
+SPLIT = """$MeshFormat
+2.2 0 8
+$EndMeshFormat
+$PhysicalNames
+3
+1 1 "Bottom"
+1 2 "Rest"
+2 3 "Flow"
+$EndPhysicalNames
+$Nodes
+4
+1 0 0 0
+2 1 0 0
+3 1 1 0
+4 0 1 0
+$EndNodes
+$Elements
+6
+1 1 2 1 1 1 2
+2 1 2 2 2 2 3
+3 1 2 2 2 3 4
+4 1 2 1 1 4 1
+5 2 2 3 3 1 3 2
+6 2 2 3 3 1 3 4
+$EndElements
+"""
+
+
+def test_gmsh_split_groups_and_clockwise_elements(tmp_path):
+    """Group 'Bottom' appears twice (merged, io.d:910-942); element 5 is clockwise (reversed, io.d:969-987)."""
+    p = write(tmp_path, "split.msh", SPLIT)
+    r = gmsh_ref.parse_gmsh(p)
+    assert r["bTags"] == ["Bottom", "Rest"]
+    assert r["bGroupStart"] == [0, 2]
+    assert [list(x) for x in r["bNodes"]] == [[0, 1], [3, 0], [1, 2], [2, 3]]
+    assert r["elements"][0] == [2, 3, 1]
+    m = E.import_mesh(p)
+    assert m.n_cells == 2 and m.tags == ["Bottom", "Rest"] and m.info.n_ghost == 4
+    assert m.info.n_int_edges == 1
+
+
+@pytest.mark.parametrize("bad,needle", [
+    ("$MeshFormat\n2.2 1 8\n$EndMeshFormat\n", "format"),
+    (SPLIT.replace("1 2 2 2 2 3", "9 2 2 2 2 3"), "element"),
+    (SPLIT.replace("5 2 2 3 3 1 3 2", "5 15 2 3 3 1"), "type"),
+    (SPLIT.replace("3 1 1 0", "3 1 1"), "node"),
+    (SPLIT.replace("$EndNodes", "$EndNodez").replace("$Elements", "$Junk"), ""),
+])
+def test_gmsh_malformed_inputs_fail_cleanly(tmp_path, bad, needle):
+    p = write(tmp_path, "bad.msh", bad)
+    with pytest.raises(E.EbbError) as ei:
+        E.import_mesh(p)
+    assert ei.value.code in (3, 4)
+
+
+def test_missing_mesh_file_is_io_error():
+    with pytest.raises(E.EbbError) as ei:
+        E.import_mesh("/nonexistent/none.msh")
+    assert ei.value.code == 2
+
+
+def test_mesh_from_arrays_and_generators():
+    g = meshgen.wedge(3000, seed=0)
+    m = g.to_solver_mesh()
+    assert m.n_cells == g.n_cells
+    assert m.tags == g.tags
+    assert m.info.n_ghost == len(g.b_nodes)
+    q = meshgen.uniform_quads(8).to_solver_mesh()
+    assert q.n_cells == 64 and q.info.n_ghost == 32 and q.info.n_int_edges == 112
+    f = meshgen.flat_plate(20000)
+    fm = f.to_solver_mesh()
+    assert fm.n_cells == f.n_cells and fm.info.max_edges == 4
+
+
+def test_solver_create_fails_loudly_without_gpu():
+    L = _lib.load()
+    n = C.c_int()
+    if L.ebb_device_count(C.byref(n)) == 0:
+        pytest.skip("a GPU is present; the no-device path is not reachable")
+    m = meshgen.uniform_quads(4).to_solver_mesh()
+    cfg = E.default_config()
+    E.set_boundaries(cfg, [("Freestream", "fullState", [0.5, 0, 1, 1])])
+    with pytest.raises(E.EbbError) as ei:
+        E.UfvmSolver(m, cfg)
+    assert ei.value.code == 10
+    with pytest.raises(E.EbbError):
+        E.roe_flux(np.ones(4), np.ones(4), [1.0, 0.0])
