@@ -103,46 +103,35 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def algorithmic_bytes(info, need_grad=False, limited=True):
+def algorithmic_bytes(info, real=8, need_grad=False, limited=True):
     """Bytes each kernel must move per launch, every array touched once (re-reads of
-    a neighbour's state count 0).  S = face slots, E = interior edges, G = boundary edges."""
+    a neighbour's state count 0).  S = face slots, E = interior edges, G = boundary
+    edges; real = bytes of the arithmetic type (8 plain FP64, 4 split)."""
     C, S, E, G = info.n_cells, info.face_slots, info.n_int_edges, info.n_ghost
-    cell = C * (32 + 4) + S * (4 + 16 + (16 if limited else 0) + 16) + S * 32 + (C * 64 if need_grad else 0)
-    flux = E * (8 + 16 + 8 + 64 + 40) + G * (12 + 16 + 8 + 32 + 32 + 40)
-    # residual + RK2 first-stage update: per cell nedge, perim, d, -1/area, q read, aux and stage-state writes
-    update = C * (4 + 24 + 32 + 32 + 32) + S * 4 + (E + G) * 40
+    r = real
+    cell = C * (4 * r + 4) + S * (4 + 2 * r + (2 * r if limited else 0) + 2 * r) + S * 4 * r + (C * 8 * r if need_grad else 0)
+    flux = E * (8 + 2 * r + r + 8 * r + 5 * r) + G * (12 + 2 * r + r + 4 * r + 4 * r + 5 * r)
+    # residual + RK2 first-stage update: nedge, perim, d, -1/area, FP64 q read, aux write
+    # (T) and next-stage state write (T)
+    update = C * (4 + 3 * r + 32 + 4 * r + 4 * r) + S * 4 + (E + G) * 5 * r
     return {"cell": cell, "flux": flux, "update": update}
 
 
-def run_ours(args, ws, rank, local):
+def measure(L, E, _lib, gen, mesh, precision, args, local, ws, want_e2e):
     import ctypes as C
-    import ebbcfd_gb300 as E
-    from ebbcfd_gb300 import _lib, meshgen
-
-    L = _lib.load()
-    L.ebb_set_device(local)
-    t0 = time.time()
-    gen = meshgen.wedge(args.cells, seed=0)
-    mesh = gen.to_solver_mesh()
     cfg = E.load_config(wedge_config())
-    sol = E.UfvmSolver(mesh, cfg)
+    t0 = time.time()
+    sol = E.UfvmSolver(mesh, cfg, precision=precision)
     setup_s = time.time() - t0
     info = mesh.info
     ncell = info.n_cells
-
-    # warm-up (also builds the CUDA graphs of the time loop)
     sol.run(args.warmup, records=False)
-
-    # per-kernel device times (CUDA events on the solver stream)
     ms = (C.c_double * 4)()
     L.ebb_profile_kernels(sol.h, 20, ms)
     kern_ms = {"cell": ms[0], "flux": ms[1], "update": ms[2], "step_end": ms[3]}
-
-    barrier = None
     if ws > 1:
         import torch.distributed as dist
-        barrier = dist.barrier
-        barrier()
+        dist.barrier()
     clocks = Clocks(local)
     clocks.start()
     n = C.c_int64()
@@ -151,27 +140,26 @@ def run_ours(args, ws, rank, local):
     clk = clocks.stop()
     if code != 0:
         sol._raise(code)
-    if barrier:
-        barrier()
     elapsed = dev_ms.value / 1e3
     steps_done = n.value
     if ws > 1:
         import torch
         import torch.distributed as dist
+        dist.barrier()
         t = torch.tensor([elapsed], dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed = float(t.item())
+    state = sol.state
     value = ws * ncell * steps_done / elapsed
-
-    # end to end through the public API with host buffers: every step uploads the state
-    # from page-locked memory, advances one step and reads the state and step record back
     e2e = None
-    if not args.no_e2e:
+    if want_e2e:
+        # end to end through the public API with host buffers: every step uploads the
+        # state from page-locked memory, advances one step and reads state and record back
         nbytes = ncell * 4 * 8
         ph = C.c_void_p()
         L.ebb_host_alloc(nbytes, C.byref(ph))
         host = np.ctypeslib.as_array((C.c_double * (ncell * 4)).from_address(ph.value)).reshape(ncell, 4)
-        L.ebb_get_state(sol.h, host.ctypes.data_as(C.POINTER(C.c_double)))
+        host[:] = state
         rec = (_lib.StepRecord * 1)()
         k_e2e = max(3, min(args.steps, 50))
         hp = host.ctypes.data_as(C.POINTER(C.c_double))
@@ -184,29 +172,55 @@ def run_ours(args, ws, rank, local):
         L.ebb_host_free(ph)
         e2e = {"value": ws * ncell * k_e2e / t_e2e, "unit": "cell-updates/s", "h2d_bytes_per_step": nbytes,
                "d2h_bytes_per_step": nbytes + C.sizeof(_lib.StepRecord), "steps": k_e2e}
-
     peak, peak_kind = peaks()
-    ab = algorithmic_bytes(info)
+    ab = algorithmic_bytes(info, real=8 if precision == "fp64" else 4)
     dom = max(("cell", "flux", "update"), key=lambda k: kern_ms[k])
     achieved = ab[dom] / (kern_ms[dom] * 1e-3) / 1e9
     roof = {"bound": "hbm", "kernel": "k_" + dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
-            "kernel_ms": kern_ms, "algorithmic_bytes": ab}
+            "frac": achieved / peak, "peak_source": peak_kind, "traffic": None, "kernel_ms": kern_ms,
+            "algorithmic_bytes": ab}
+    sol.close()
+    return {"value": value, "elapsed": elapsed, "steps": steps_done, "setup_s": setup_s, "roofline": roof,
+            "e2e": e2e, "clocks": clk, "state": state}
 
+
+def run_ours(args, ws, rank, local):
+    import ebbcfd_gb300 as E
+    from ebbcfd_gb300 import _lib, meshgen
+
+    L = _lib.load()
+    L.ebb_set_device(local)
+    t0 = time.time()
+    gen = meshgen.wedge(args.cells, seed=0)
+    mesh = gen.to_solver_mesh()
+    mesh_s = time.time() - t0
+    info = mesh.info
+    ncell = info.n_cells
+    m64 = measure(L, E, _lib, gen, mesh, "fp64", args, local, ws, not args.no_e2e)
+    split = None
+    if not args.no_split:
+        m32 = measure(L, E, _lib, gen, mesh, "split", args, local, ws, False)
+        q64, q32 = m64["state"], m32["state"]
+        scale = np.maximum(np.abs(q64).max(axis=0), 1e-300)
+        split = {"value": m32["value"], "unit": "cell-updates/s", "ms_per_step": 1e3 * m32["elapsed"] / m32["steps"],
+                 "speedup_vs_fp64": m32["value"] / m64["value"], "roofline": m32["roofline"],
+                 "state_rel_err_vs_fp64": float((np.abs(q32 - q64).max(axis=0) / scale).max()),
+                 "steps_compared": m64["steps"] + args.warmup, "clocks": m32["clocks"]}
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(gen, ncell, budget_s=args.cpu_budget)
-
+    steps_done = m64["steps"]
     out = {
-        "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": steps_done,
-        "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / max(1, steps_done), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "metric": "cell-updates/s", "value": m64["value"], "unit": "cell-updates/s", "n_gpus": ws,
+        "steps": steps_done, "warmup": args.warmup, "ms_per_step": 1e3 * m64["elapsed"] / max(1, steps_done),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "wedge-M2.5-rusanov-rk2-cfl0.4", "cells": ncell, "faces": info.face_slots,
                    "interior_edges": info.n_int_edges, "boundary_edges": info.n_ghost, "precision": "plain-fp64",
                    "l2": "inputs larger than L2 (~%d MB resident)" % (sol_bytes(info) // 2 ** 20),
-                   "parallelism": "replicas" if ws > 1 else "single", "setup_s": round(setup_s, 2)},
-        "cell_stages_per_s": 2 * value, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
-        "gpu_launches": steps_done * 7, "clocks": clk,
+                   "parallelism": "replicas" if ws > 1 else "single", "mesh_s": round(mesh_s, 2),
+                   "setup_s": round(m64["setup_s"], 2)},
+        "cell_stages_per_s": 2 * m64["value"], "roofline": m64["roofline"], "cpu_baseline": cpu,
+        "e2e": m64["e2e"], "gpu_launches": steps_done * 7, "clocks": m64["clocks"], "split_path": split,
     }
     return out
 
@@ -270,6 +284,7 @@ def main():
     ap.add_argument("--cells", type=int, default=1_000_000)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-split", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)

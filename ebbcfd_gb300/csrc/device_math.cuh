@@ -22,6 +22,19 @@ template <> struct K<float> {
 
 template <typename T> __device__ __forceinline__ T dsqrt(T x) { return sqrt(x); }
 template <> __device__ __forceinline__ float dsqrt<float>(float x) { return sqrtf(x); }
+template <typename T> __device__ __forceinline__ T dpow(T x, T y) { return pow(x, y); }
+template <> __device__ __forceinline__ float dpow<float>(float x, float y) { return powf(x, y); }
+
+// Binary exponent of |x| (biased by 1023), read on the integer pipe; 0x7ff for inf/NaN.
+__device__ __forceinline__ int bexp(double x) { return (__double2hiint(x) >> 20) & 0x7ff; }
+// x finite and 2^-60 <= |x| < 2^60 (and positive when pos)
+__device__ __forceinline__ bool mid_range(double x, bool pos)
+{
+    const int h = __double2hiint(x);
+    const int e = (h >> 20) & 0x7ff;
+    return e >= 1023 - 60 && e < 1023 + 60 && (!pos || h >= 0);
+}
+__device__ __forceinline__ bool bounded(double x) { return bexp(x) < 1023 + 60; }
 
 // source/euler.d:91-94
 template <typename T> __device__ __forceinline__ T pressure(const T q[4])
@@ -29,6 +42,24 @@ template <typename T> __device__ __forceinline__ T pressure(const T q[4])
     T a = q[1] / q[0], b = q[2] / q[0];
     return K<T>::gm1 * (q[3] - T(0.5) * q[0] * (a * a + b * b));
 }
+
+// Sign of source/euler.d:91-94's pressure without its two divisions.  The reference
+// value is gm1 * (q3 - Y) with Y = 0.5 q0 ((q1/q0)^2 + (q2/q0)^2) rounded within 7 units
+// in the last place; q0 q3 - 0.5 (q1^2 + q2^2) has the same sign as q3 - Y whenever it
+// exceeds 2^-44 of its terms' magnitude (>= 32x the combined rounding bound), for
+// states within [2^-60, 2^60].  Anything closer to zero, or outside that range, takes
+// the reference's own expression, so the decision is always the reference's.
+__device__ __forceinline__ bool pressure_negative(const double q[4])
+{
+    if (mid_range(q[0], true) && mid_range(q[3], true) && bounded(q[1]) && bounded(q[2])) {
+        double W = q[3] * q[0];
+        double Z = 0.5 * (q[1] * q[1] + q[2] * q[2]);
+        double d = W - Z;
+        if (fabs(d) > 0x1p-44 * (W + Z)) return d < 0;
+    }
+    return pressure(q) < 0;
+}
+__device__ __forceinline__ bool pressure_negative(const float q[4]) { return pressure(q) < 0; }
 
 // source/flux.d:19-24
 template <typename T>
@@ -113,7 +144,66 @@ __device__ __forceinline__ void roe_flux(const T qL[4], const T qR[4], T nx, T n
 
 // source/flux.d:66-141 (Roe-type averaged speed; every wave set to sMax)
 template <typename T>
+__device__ __forceinline__ void rusanov_flux_full(const T qL[4], const T qR[4], T nx, T ny, T out[4], T &sMax);
+
+// With every wave speed equal to sMax the reference's s1 - sMax and s2 are exact
+// zeros, so its C1 and C2 terms are signed zeros whenever G1/a^2, G2/a and G1/a are
+// finite, and the flux reduces to 0.5 (fL + fR) - 0.5 sMax (qR - qL) bit for bit (up
+// to the sign of exact zeros).  That holds for densities, states and sound speeds in
+// the ranges checked below (integer-pipe exponent tests); outside them the full
+// expression runs.  Single precision computes the reduced form directly.
+template <typename T>
 __device__ __forceinline__ void rusanov_flux(const T qL[4], const T qR[4], T nx, T ny, T out[4], T &sMax)
+{
+    if (sizeof(T) == 8) {
+        const double *a = reinterpret_cast<const double *>(qL), *b = reinterpret_cast<const double *>(qR);
+        bool ok = mid_range(a[0], true) && mid_range(b[0], true) && bounded(a[1]) && bounded(a[2]) &&
+                  bounded(a[3]) && bounded(b[1]) && bounded(b[2]) && bounded(b[3]);
+        if (!ok) {
+            rusanov_flux_full(qL, qR, nx, ny, out, sMax);
+            return;
+        }
+    }
+    const T gm1 = K<T>::gm1;
+    T rhoL = qL[0], uL = qL[1] / rhoL, vL = qL[2] / rhoL;
+    T pL = gm1 * (qL[3] - T(0.5) * rhoL * (uL * uL + vL * vL));
+    T rhoR = qR[0], uR = qR[1] / rhoR, vR = qR[2] / rhoR;
+    T pR = gm1 * (qR[3] - T(0.5) * rhoR * (uR * uR + vR * vR));
+    T rho = dsqrt(rhoL * rhoR);
+    T sL = dsqrt(rhoL), sR = dsqrt(rhoR);
+    T vel0 = (sL * uL + sR * uR) / (sL + sR);
+    T vel1 = (sL * vL + sR * vR) / (sL + sR);
+    T u = vel0 * nx + vel1 * ny;
+    T p = (sL * pL + sR * pR) / (sL + sR);
+    T a = dsqrt(K<T>::g * (p / rho));
+    if (sizeof(T) == 8) {
+        const int e = bexp((double)a);
+        if (!(e >= 1023 - 200 && e < 1023 + 100)) {
+            rusanov_flux_full(qL, qR, nx, ny, out, sMax);
+            return;
+        }
+    }
+    T lam1 = fabs(u + a), lam2 = fabs(u - a), lam3 = fabs(u);
+    T eps = T(0.01) * a;
+    lam1 = entropy_fix(lam1, eps);
+    lam2 = entropy_fix(lam2, eps);
+    lam3 = entropy_fix(lam3, eps);
+    T sm = max4(fabs(lam1), fabs(lam2), fabs(lam3), fabs(lam3));
+    sMax = sm;
+    T fL[4], fR[4];
+    convective_flux(pL, uL, vL, rhoL, qL[3], nx, ny, fL);
+    convective_flux(pR, uR, vR, rhoR, qR[3], nx, ny, fR);
+    T dRho = rhoR - rhoL;
+    T dRV0 = rhoR * uR - rhoL * uL, dRV1 = rhoR * vR - rhoL * vL;
+    T dRhoE = qR[3] - qL[3];
+    out[0] = T(0.5) * (fL[0] + fR[0]) - T(0.5) * (sm * dRho);
+    out[1] = T(0.5) * (fL[1] + fR[1]) - T(0.5) * (sm * dRV0);
+    out[2] = T(0.5) * (fL[2] + fR[2]) - T(0.5) * (sm * dRV1);
+    out[3] = T(0.5) * (fL[3] + fR[3]) - T(0.5) * (sm * dRhoE);
+}
+
+template <typename T>
+__device__ __forceinline__ void rusanov_flux_full(const T qL[4], const T qR[4], T nx, T ny, T out[4], T &sMax)
 {
     const T gm1 = K<T>::gm1;
     T rhoL = qL[0], uL = qL[1] / rhoL, vL = qL[2] / rhoL;

@@ -1,0 +1,882 @@
+// kernels.cuh -- the explicit unstructured FV update as three kernels per stage,
+// templated on the arithmetic type T:
+//   T = double  plain FP64 path (k_fp64.cu, compiled without multiply-add contraction:
+//               the reference's operation order, bitwise its results);
+//   T = float   split path (k_split.cu): FP32 face, flux, gradient and limiter
+//               arithmetic on FP32 copies of the FP64 geometry; the solution, the
+//               u += dt R updates and the norm/force reductions stay FP64.
+//
+//   k_cell    one thread per interior cell: ghost states of its boundary faces
+//             (solve.d:521-689), least-squares gradient and neighbour min/max
+//             (solve.d:329-358), scalar and LP limiters (solve.d:360-497), and the
+//             reconstructed state of each of its faces with the negative-pressure
+//             fallback (solve.d:283-319,980-1011), written to that face's slot.
+//   k_flux    one thread per edge: interior Roe/Rusanov (+viscous) flux from the two
+//             face slots (solve.d:970-1033), boundary fluxes per BC (solve.d:769-968);
+//             stores len*F and len*sMax once per edge.
+//   k_update  one thread per interior cell: gathers its edges' len*F with the
+//             +-1 multipliers in the cell's own edge order (the reference's summation
+//             order), CFL time step, Rmax, -1/area scaling (solve.d:1080-1121), the
+//             manufactured source, and the integrator stage combination
+//             (integrators.d), with min/max/sum reductions in fixed-order trees.
+// Accumulation is atomic-free (gather, not scatter); the only atomics are the
+// order-independent min/max of dt and Rmax and the first-error key.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "device_math.cuh"
+#include "layout.h"
+
+namespace ebbdev {
+
+constexpr int BC_FULLSTATE = 0, BC_CONSTP = 1, BC_INVWALL = 2, BC_VISCWALL = 3, BC_SYMMETRY = 4, BC_TPINFLOW = 5,
+              BC_DIRICHLET = 6;
+constexpr int BC_VERTICAL = 0x100;  // flag: reflection across a vertical edge (x1 == x2)
+constexpr int ERR_NAN_EDGE = 8, ERR_NAN_CELL = 9, ERR_BC = 11;
+constexpr int UPD_THREADS = 256;
+
+__device__ __forceinline__ bool halted(const DState *st) { return st->done || st->err_key != EBB_NOERR; }
+
+__device__ __forceinline__ void flag_error(DState *st, unsigned phase, unsigned code, unsigned idx)
+{
+    unsigned long long key = ((unsigned long long)phase << 48) | ((unsigned long long)code << 40) | idx;
+    atomicMin(&st->err_key, key);
+}
+
+// 4-vector loads/stores: two 16-byte accesses for double, one for float
+__device__ __forceinline__ void ld4(const double *p, double v[4])
+{
+    const double2 *q = reinterpret_cast<const double2 *>(p);
+    double2 a = q[0], b = q[1];
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = b.x;
+    v[3] = b.y;
+}
+__device__ __forceinline__ void st4(double *p, const double v[4])
+{
+    double2 *q = reinterpret_cast<double2 *>(p);
+    q[0] = make_double2(v[0], v[1]);
+    q[1] = make_double2(v[2], v[3]);
+}
+__device__ __forceinline__ void ld4(const float *p, float v[4])
+{
+    float4 a = *reinterpret_cast<const float4 *>(p);
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = a.z;
+    v[3] = a.w;
+}
+__device__ __forceinline__ void st4(float *p, const float v[4])
+{
+    *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+template <typename T> struct V2;
+template <> struct V2<double> {
+    using t = double2;
+};
+template <> struct V2<float> {
+    using t = float2;
+};
+template <typename T> __device__ __forceinline__ typename V2<T>::t ld2(const void *base, size_t i)
+{
+    return reinterpret_cast<const typename V2<T>::t *>(base)[i];
+}
+template <typename T> __device__ __forceinline__ T ld1(const void *base, size_t i)
+{
+    return reinterpret_cast<const T *>(base)[i];
+}
+template <typename T> __device__ __forceinline__ const T *ptr(const void *base) { return reinterpret_cast<const T *>(base); }
+
+template <typename T>
+__device__ __forceinline__ void reflect(int type, const T *refl, T v0, T v1, T &o0, T &o1)
+{
+    if (type & BC_VERTICAL) {
+        o0 = -v0;
+        o1 = v1;
+    } else {
+        o0 = refl[0] * v0 + refl[1] * v1;
+        o1 = refl[2] * v0 + refl[3] * v1;
+    }
+}
+
+// ghost state of boundary edge b from the owner's state qi (solve.d:521-689)
+template <typename T>
+__device__ void ghost_state(const DMesh &M, const DPhys &P, DState *st, int b, const T qi[4], T qn[4])
+{
+    const int type = M.b_type[b];
+    const T G = K<T>::g;
+    switch (type & 0xff) {
+    case BC_DIRICHLET:
+        ld4(ptr<T>(M.g.b_dq) + 4 * (size_t)b, qn);
+        break;
+    case BC_FULLSTATE:
+        for (int k = 0; k < 4; k++) qn[k] = qi[k];
+        break;
+    case BC_INVWALL:
+    case BC_SYMMETRY: {
+        T v0 = qi[1] / qi[0], v1 = qi[2] / qi[0], n0, n1;
+        reflect(type, ptr<T>(M.g.b_refl) + 4 * (size_t)b, v0, v1, n0, n1);
+        qn[0] = qi[0];
+        qn[1] = qi[0] * n0;
+        qn[2] = qi[0] * n1;
+        qn[3] = qi[3];
+        break;
+    }
+    case BC_VISCWALL:
+        qn[0] = qi[0];
+        qn[1] = -qi[1];
+        qn[2] = -qi[2];
+        qn[3] = qi[3];
+        break;
+    case BC_CONSTP: {
+        T rhop = qi[0], up = qi[1] / qi[0], vp = qi[2] / qi[0];
+        T pp = pressure(qi);
+        T ap = dsqrt(G * (pp / rhop));
+        T Jp = up + (T(2.0) * ap) / (G - 1);
+        T Sp = pp / dpow(rhop, G);
+        T pb = ptr<T>(M.g.b_data)[4 * (size_t)b];
+        T rhob = dpow(pb / Sp, T(1.0 / 1.4));
+        T ab = dsqrt(G * (pb / rhob));
+        T ub = Jp - (T(2.0) * ab) / (G - 1);
+        T vb = vp;
+        T mag = dsqrt(ub * ub + vb * vb);
+        T rEb = pb / (G - 1) + T(0.5) * rhob * (mag * mag);
+        const typename V2<T>::t n = ld2<T>(M.g.b_n, b);
+        T vpn = up * n.x + vp * n.y;
+        T vbn = ub * n.x + vb * n.y;
+        T g0 = up - vpn * n.x + vbn * n.x;
+        T g1 = vp - vpn * n.y + vbn * n.y;
+        qn[0] = rhob;
+        qn[1] = rhob * g0;
+        qn[2] = rhob * g1;
+        qn[3] = rEb;
+        break;
+    }
+    case BC_TPINFLOW: {
+        const T *bd = ptr<T>(M.g.b_data) + 4 * (size_t)b;
+        T Tt = bd[0], Pt = bd[1], nin0 = bd[2], nin1 = bd[3];
+        T rhop = qi[0], up = qi[1] / qi[0];
+        T pp = pressure(qi);
+        T ap = dsqrt(G * (pp / rhop));
+        T Jp = up + (T(2.0) * ap) / (G - 1);
+        const typename V2<T>::t n = ld2<T>(M.g.b_n, b);
+        T d = nin0 * n.x + nin1 * n.y;
+        T Rg = (T)P.r_gas;
+        T aa = G * Rg * Tt * (d * d) - T(0.5) * (G - 1) * (Jp * Jp);
+        T bb = (T(4.0) * G * Rg * Tt * d) / (G - 1);
+        T cc = (T(4.0) * G * Rg * Tt) / ((G - 1) * (G - 1)) - Jp * Jp;
+        T M1 = (-bb + dsqrt(bb * bb - 4 * aa * cc)) / (T(2.0) * aa);
+        T M2 = (-bb - dsqrt(bb * bb - 4 * aa * cc)) / (T(2.0) * aa);
+        T Mb = 0;
+        if (M1 >= 0 && M2 >= 0)
+            Mb = fmin(M1, M2);
+        else if (M1 >= 0 && M2 < 0)
+            Mb = M1;
+        else if (M1 < 0 && M2 >= 0)
+            Mb = M2;
+        else
+            flag_error(st, 0, ERR_BC, (unsigned)M.b_ref[b]);
+        T Tb = Tt / (1 + T(0.5) * (G - 1) * (Mb * Mb));
+        T pb = Pt * dpow(Tb / Tt, G / (G - 1));
+        T rhob = pb / (Rg * Tb);
+        T ab = dsqrt(G * (pb / rhob));
+        T vb0 = Mb * ab * nin0, vb1 = Mb * ab * nin1;
+        T mag = dsqrt(vb0 * vb0 + vb1 * vb1);
+        T rEb = pb / (G - 1) + T(0.5) * rhob * (mag * mag);
+        // solve.d:678-681 writes every value into component 0; the other
+        // components of the ghost slot are never written and stay zero
+        qn[0] = rEb;
+        qn[1] = 0;
+        qn[2] = 0;
+        qn[3] = 0;
+        break;
+    }
+    default:
+        for (int k = 0; k < 4; k++) qn[k] = qi[k];
+    }
+}
+
+// LP!m (solve.d:37-173) on the m = 4 + 2*nNb constraints of solve.d:404-497
+template <typename T>
+__device__ __forceinline__ void lp_limit(const DMesh &M, int i, int ne, const T qi[4], const T mn[4], const T mx[4],
+                                         const T g[4][2], T lim0[4], T lim1[4], T thresh)
+{
+#pragma unroll 1
+    for (int k = 0; k < 4; k++) {
+        if (!(lim0[k] < thresh) || !(ne == 3 || ne == 4)) continue;
+        T A[12][2], b[12];
+        int mr = 4 + 2 * ne;
+        A[0][0] = 1;
+        A[0][1] = 0;
+        A[1][0] = 0;
+        A[1][1] = 1;
+        A[2][0] = -1;
+        A[2][1] = 0;
+        A[3][0] = 0;
+        A[3][1] = -1;
+        b[0] = 0;
+        b[1] = 0;
+        b[2] = -1;
+        b[3] = -1;
+        for (int j = 0; j < ne; j++) {
+            const typename V2<T>::t nd = ld2<T>(M.g.s_nd, (size_t)j * M.Cs + i);
+            A[2 * j + 4][0] = nd.x * g[k][0];
+            A[2 * j + 4][1] = nd.y * g[k][1];
+            b[2 * j + 4] = mn[k] - qi[k];
+            A[2 * j + 5][0] = -nd.x * g[k][0];
+            A[2 * j + 5][1] = -nd.y * g[k][1];
+            b[2 * j + 5] = qi[k] - mx[k];
+        }
+        T c0 = -fabs(g[k][0]), c1 = -fabs(g[k][1]);
+        T xk0 = 0, xk1 = 0;
+        int W0 = 0, W1 = 1;
+        T Ak[4] = {A[0][0], A[0][1], A[1][0], A[1][1]};
+        for (int it = 0;;) {
+            T det = Ak[0] * Ak[3] - Ak[1] * Ak[2];
+            T id = T(1.0) / det;
+            T l0 = (Ak[3] * id) * c0 + (-Ak[2] * id) * c1;
+            T l1 = (-Ak[1] * id) * c0 + (Ak[0] * id) * c1;
+            if ((l0 >= T(-10e-9)) && (l1 >= T(-10e-9))) break;
+            int qi_ = (l0 < l1) ? W0 : W1;
+            T e0 = (l0 < l1) ? 1 : 0, e1 = (l0 < l1) ? 0 : 1;
+            T pk0 = (Ak[3] * id) * e0 + (-Ak[1] * id) * e1;
+            T pk1 = (-Ak[2] * id) * e0 + (Ak[0] * id) * e1;
+            T alpha = INFINITY;
+            int t = 0;
+            T gam[12];
+            int D[12], Dlen = 0;
+            for (int r = 0; r < mr; r++)
+                if (r != W0 && r != W1)
+                    if (A[r][0] * pk0 + A[r][1] * pk1 < T(-1e-11)) D[Dlen++] = r;
+            for (int r = 0; r < Dlen; r++) {
+                T aixk = A[D[r]][0] * xk0 + A[D[r]][1] * xk1;
+                T aipk = A[D[r]][0] * pk0 + A[D[r]][1] * pk1;
+                gam[r] = (aixk - b[D[r]]) / (-aipk);
+                alpha = fmin(alpha, gam[r]);
+            }
+            for (int r = 0; r < Dlen; r++)
+                if (gam[r] == alpha) {
+                    t = D[r];
+                    break;
+                }
+            if (qi_ == W0)
+                W0 = t;
+            else if (qi_ == W1)
+                W1 = t;
+            Ak[0] = A[W0][0];
+            Ak[1] = A[W0][1];
+            Ak[2] = A[W1][0];
+            Ak[3] = A[W1][1];
+            xk0 += alpha * pk0;
+            xk1 += alpha * pk1;
+            if (++it > 15) break;
+        }
+        lim0[k] = xk0;
+        lim1[k] = xk1;
+    }
+}
+
+template <typename T, int MJ, bool LP>
+__global__ void __launch_bounds__(128) k_cell(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, int limit)
+{
+    if (halted(A.st)) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M.C) return;
+    const int Cs = M.Cs;
+    T *qghost = const_cast<T *>(qin);  // ghost slots [C, C+G) are written by their owner only
+    T qi[4];
+    ld4(qin + 4 * (size_t)i, qi);
+    const int ne = M.nedge[i];
+    T mn[4], mx[4], g[4][2];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        mn[k] = qi[k];
+        mx[k] = qi[k];
+        g[k][0] = T(0.0);
+        g[k][1] = T(0.0);
+    }
+    const bool second = P.order > 1;
+#pragma unroll
+    for (int j = 0; j < MJ; j++) {
+        if (j < ne) {
+            const size_t s = (size_t)j * Cs + i;
+            const int nb = M.s_nbr[s];
+            T qn[4];
+            if (nb < M.C) {
+                ld4(qin + 4 * (size_t)nb, qn);
+            } else {
+                ghost_state<T>(M, P, A.st, nb - M.C, qi, qn);
+                st4(qghost + 4 * (size_t)nb, qn);
+            }
+            if (second) {
+                const typename V2<T>::t gm = ld2<T>(M.g.s_gm, s);
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    mn[k] = fmin(mn[k], qn[k]);
+                    mx[k] = fmax(mx[k], qn[k]);
+                    T du = qn[k] - qi[k];
+                    g[k][0] = g[k][0] + gm.x * du;
+                    g[k][1] = g[k][1] + gm.y * du;
+                }
+            }
+        }
+    }
+    T lim0[4] = {T(1.0), T(1.0), T(1.0), T(1.0)}, lim1[4] = {T(1.0), T(1.0), T(1.0), T(1.0)};
+    if (second && P.limited && limit) {
+#pragma unroll
+        for (int j = 0; j < MJ; j++) {
+            if (j < ne) {
+                const typename V2<T>::t nd = ld2<T>(M.g.s_nd, (size_t)j * Cs + i);
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    T s = T(1.0);
+                    T qE = qi[k] + (g[k][0] * nd.x + g[k][1] * nd.y);
+                    if (qE < mn[k])
+                        s = (mn[k] - qi[k]) / (g[k][0] * nd.x + g[k][1] * nd.y);
+                    else if (qE > mx[k])
+                        s = (mx[k] - qi[k]) / (g[k][0] * nd.x + g[k][1] * nd.y);
+                    lim0[k] = fmin(lim0[k], s);
+                    lim1[k] = lim0[k];
+                }
+            }
+        }
+        if (LP) lp_limit<T>(M, i, ne, qi, mn, mx, g, lim0, lim1, (T)P.lp_thresh);
+    }
+    if (P.need_grad) {
+        T *gp = reinterpret_cast<T *>(A.grad) + 8 * (size_t)i;
+        if (second) {
+            T a[4] = {g[0][0], g[0][1], g[1][0], g[1][1]}, b[4] = {g[2][0], g[2][1], g[3][0], g[3][1]};
+            st4(gp, a);
+            st4(gp + 4, b);
+        } else {  // order 1: interior gradients are never computed (NaN-initialised in the reference)
+            T nanv[4] = {T(NAN), T(NAN), T(NAN), T(NAN)};
+            st4(gp, nanv);
+            st4(gp + 4, nanv);
+        }
+    }
+    T lg0[4], lg1[4];
+    T l0 = T(1.0), l1 = T(1.0);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        lg0[k] = lim0[k] * g[k][0];
+        lg1[k] = lim1[k] * g[k][1];
+        l0 = fmin(l0, lim0[k]);
+        l1 = fmin(l1, lim1[k]);
+    }
+    T *face = reinterpret_cast<T *>(A.face);
+#pragma unroll
+    for (int j = 0; j < MJ; j++) {
+        if (j < ne) {
+            const size_t s = (size_t)j * Cs + i;
+            T f[4];
+            if (!second) {
+#pragma unroll
+                for (int k = 0; k < 4; k++) f[k] = qi[k];
+            } else {
+                const typename V2<T>::t fd = ld2<T>(M.g.s_fd, s);
+#pragma unroll
+                for (int k = 0; k < 4; k++) f[k] = qi[k] + lg0[k] * fd.x + lg1[k] * fd.y;
+                if (pressure_negative(f)) {
+                    const int ev = M.s_edge[s] & 0x7fffffff;
+                    const T ll1 = (ev >= M.Eint) ? l0 : l1;  // updateBoundaryEdge uses lim[0] twice
+#pragma unroll
+                    for (int k = 0; k < 4; k++) f[k] = qi[k] + l0 * g[k][0] * fd.x + ll1 * g[k][1] * fd.y;
+                }
+            }
+            st4(face + 4 * s, f);
+        }
+    }
+}
+
+template <typename T> __device__ __forceinline__ void load_grad(const void *grad, int c, T g[4][2])
+{
+    T a[4], b[4];
+    const T *p = reinterpret_cast<const T *>(grad) + 8 * (size_t)c;
+    ld4(p, a);
+    ld4(p + 4, b);
+    g[0][0] = a[0];
+    g[0][1] = a[1];
+    g[1][0] = a[2];
+    g[1][1] = a[3];
+    g[2][0] = b[0];
+    g[2][1] = b[1];
+    g[3][0] = b[2];
+    g[3][1] = b[3];
+}
+
+template <typename T> __device__ __forceinline__ bool has_nan(const T F[4])
+{
+    return isnan(F[0]) || isnan(F[1]) || isnan(F[2]) || isnan(F[3]);
+}
+
+template <typename T>
+__device__ void boundary_flux(const DMesh &M, const DPhys &P, const DArrays &A, const T *qin, int b)
+{
+    const T G = K<T>::g;
+    const int type = M.b_type[b];
+    const size_t fsl = (size_t)M.b_slot[b];
+    T qL[4];
+    ld4(reinterpret_cast<const T *>(A.face) + 4 * fsl, qL);
+    const typename V2<T>::t n = ld2<T>(M.g.b_n, b);
+    const T nx = n.x, ny = n.y;
+    T F[4], sMax = 0;
+    const int owner = M.b_cell[b];
+    const int ghost = M.C + b;
+    const T pr = (T)P.pr, mu = (T)P.mu;
+    switch (type & 0xff) {
+    case BC_DIRICHLET:
+    case BC_FULLSTATE: {
+        T qR[4];
+        ld4(ptr<T>((type & 0xff) == BC_DIRICHLET ? M.g.b_dmid : M.g.b_data) + 4 * (size_t)b, qR);
+        inviscid_flux(P.flux, qL, qR, nx, ny, F, sMax);
+        if (P.viscous) {
+            T g1[4][2], g2[4][2], dq[4][2], qa[4], Fv[4];
+            load_grad<T>(A.grad, owner, g1);
+            load_grad<T>(A.grad, ghost, g2);
+            for (int k = 0; k < 4; k++) {
+                qa[k] = T(0.5) * (qL[k] + qR[k]);
+                dq[k][0] = T(0.5) * (g1[k][0] + g2[k][0]);
+                dq[k][1] = T(0.5) * (g1[k][1] + g2[k][1]);
+            }
+            diffusive_flux(pr, mu, qa, dq, nx, ny, Fv);
+            for (int k = 0; k < 4; k++) F[k] = F[k] - Fv[k];
+        }
+        break;
+    }
+    case BC_INVWALL: {
+        T inv = 1 / qL[0];
+        T vp0 = inv * qL[1], vp1 = inv * qL[2];
+        T vn = vp0 * nx + vp1 * ny;
+        T t0 = vp0 - vn * nx, t1 = vp1 - vn * ny;
+        T vel = dsqrt(t0 * t0 + t1 * t1);
+        T p = (G - 1) * (qL[3] - T(0.5) * qL[0] * (vel * vel));
+        T a = dsqrt(G * (p / qL[0]));
+        if (p < 0) p = T(1.0e-12);
+        F[0] = 0;
+        F[1] = p * nx;
+        F[2] = p * ny;
+        F[3] = 0;
+        sMax = fabs(a);
+        break;
+    }
+    case BC_VISCWALL: {
+        T vel = 0.0;
+        T p = (G - 1) * (qL[3] - T(0.5) * qL[0] * (vel * vel));
+        T a = dsqrt(G * (p / qL[0]));
+        if (p < 0) p = T(1.0e-12);
+        T qR[4] = {qL[0], qL[1] * -1, qL[2] * -1, qL[3]};
+        T qa[4], dq[4][2], Fv[4];
+        for (int k = 0; k < 4; k++) qa[k] = T(0.5) * (qL[k] + qR[k]);
+        qa[1] = 0.0;
+        qa[2] = 0.0;
+        load_grad<T>(A.grad, owner, dq);
+        dq[3][0] = (qa[3] / qa[0]) * dq[0][0];
+        dq[3][1] = (qa[3] / qa[0]) * dq[0][1];
+        diffusive_flux(pr, mu, qa, dq, nx, ny, Fv);
+        F[0] = 0 - Fv[0];
+        F[1] = p * nx - Fv[1];
+        F[2] = p * ny - Fv[2];
+        F[3] = 0 - Fv[3];
+        sMax = fabs(a);
+        break;
+    }
+    case BC_CONSTP: {
+        T qg[4];
+        ld4(qin + 4 * (size_t)ghost, qg);
+        T p = pressure(qg);
+        T u = qg[1] / qg[0], v = qg[2] / qg[0];
+        T a = dsqrt(G * (p / qg[0]));
+        convective_flux(p, u, v, qg[0], qg[3], nx, ny, F);
+        sMax = fabs(a);
+        break;
+    }
+    case BC_SYMMETRY: {
+        T v0 = qL[1] / qL[0], v1 = qL[2] / qL[0], n0, n1;
+        reflect(type, ptr<T>(M.g.b_refl) + 4 * (size_t)b, v0, v1, n0, n1);
+        T qR[4] = {qL[0], qL[0] * n0, qL[0] * n1, qL[3]};
+        inviscid_flux(P.flux, qL, qR, nx, ny, F, sMax);
+        if (P.viscous) {
+            T gp[4][2], qa[4], Fv[4];
+            load_grad<T>(A.grad, owner, gp);
+            for (int k = 0; k < 4; k++) qa[k] = T(0.5) * (qL[k] + qR[k]);
+            // bGrad = gradp*nOuter + (A*gradp)*(I - 2 nOuter), solve.d:913-925
+            T nO[2][2] = {{nx * nx, nx * ny}, {ny * nx, ny * ny}};
+            T Am[4][4] = {{1, 0, 0, 0}, {0, 1 - nO[0][0], 0 - nO[0][1], 0}, {0, 0 - nO[1][0], 1 - nO[1][1], 0},
+                          {0, 0, 0, 1}};
+            T t2[2][2] = {{1 - 2 * nO[0][0], 0 - 2 * nO[0][1]}, {0 - 2 * nO[1][0], 1 - 2 * nO[1][1]}};
+            T t1[4][2], bG[4][2];
+            for (int r = 0; r < 4; r++)
+                for (int c = 0; c < 2; c++) {
+                    T acc = 0.0;
+                    for (int k = 0; k < 4; k++) acc += Am[r][k] * gp[k][c];
+                    t1[r][c] = acc;
+                }
+            for (int r = 0; r < 4; r++)
+                for (int c = 0; c < 2; c++) {
+                    T a3 = 0.0;
+                    for (int k = 0; k < 2; k++) a3 += t1[r][k] * t2[k][c];
+                    T a1 = 0.0;
+                    for (int k = 0; k < 2; k++) a1 += gp[r][k] * nO[k][c];
+                    bG[r][c] = a1 + a3;
+                }
+            diffusive_flux(pr, mu, qa, bG, nx, ny, Fv);
+            for (int k = 0; k < 4; k++) F[k] = F[k] - Fv[k];
+        }
+        break;
+    }
+    case BC_TPINFLOW: {
+        T qR[4];
+        ld4(qin + 4 * (size_t)ghost, qR);
+        inviscid_flux(P.flux, qL, qR, nx, ny, F, sMax);
+        if (P.viscous) {
+            T gp[4][2], qa[4], Fv[4];
+            load_grad<T>(A.grad, owner, gp);
+            for (int k = 0; k < 4; k++) qa[k] = T(0.5) * (qL[k] + qR[k]);
+            diffusive_flux(pr, mu, qa, gp, nx, ny, Fv);
+            for (int k = 0; k < 4; k++) F[k] = F[k] - Fv[k];
+        }
+        break;
+    }
+    default:
+        F[0] = F[1] = F[2] = F[3] = T(NAN);
+    }
+    if (has_nan(F)) flag_error(A.st, 1, ERR_NAN_EDGE, (unsigned)M.b_ref[b]);
+    const T len = ld1<T>(M.g.b_len, b);
+    const size_t e = (size_t)M.Eint + b;
+    T lf[4] = {len * F[0], len * F[1], len * F[2], len * F[3]};
+    st4(reinterpret_cast<T *>(A.fl) + 4 * e, lf);
+    reinterpret_cast<T *>(A.fs)[e] = len * sMax;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_flux(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, int nbi)
+{
+    if (halted(A.st)) return;
+    if ((int)blockIdx.x >= nbi) {
+        const int b = (blockIdx.x - nbi) * blockDim.x + threadIdx.x;
+        if (b < M.G) boundary_flux<T>(M, P, A, qin, b);
+        return;
+    }
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= M.Eint) return;
+    const int2 sl = reinterpret_cast<const int2 *>(M.e_slot)[e];
+    const T *face = reinterpret_cast<const T *>(A.face);
+    T qL[4], qR[4], F[4], sMax;
+    ld4(face + 4 * (size_t)sl.x, qL);
+    ld4(face + 4 * (size_t)sl.y, qR);
+    const typename V2<T>::t n = ld2<T>(M.g.e_n, e);
+    inviscid_flux(P.flux, qL, qR, n.x, n.y, F, sMax);
+    if (P.viscous) {
+        const int2 c = reinterpret_cast<const int2 *>(M.e_cell)[e];
+        T g1[4][2], g2[4][2], dq[4][2], qa[4], Fv[4];
+        load_grad<T>(A.grad, c.x, g1);
+        load_grad<T>(A.grad, c.y, g2);
+        for (int k = 0; k < 4; k++) {
+            qa[k] = T(0.5) * (qL[k] + qR[k]);
+            dq[k][0] = T(0.5) * (g1[k][0] + g2[k][0]);
+            dq[k][1] = T(0.5) * (g1[k][1] + g2[k][1]);
+        }
+        diffusive_flux((T)P.pr, (T)P.mu, qa, dq, n.x, n.y, Fv);
+        for (int k = 0; k < 4; k++) F[k] = F[k] - Fv[k];
+    }
+    if (has_nan(F)) flag_error(A.st, 2, ERR_NAN_EDGE, (unsigned)M.e_ref[e]);
+    const T len = ld1<T>(M.g.e_len, e);
+    T lf[4] = {len * F[0], len * F[1], len * F[2], len * F[3]};
+    st4(reinterpret_cast<T *>(A.fl) + 4 * (size_t)e, lf);
+    reinterpret_cast<T *>(A.fs)[e] = len * sMax;
+}
+
+// ---- fixed-order block reductions -------------------------------------------
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = v + __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_min(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_down_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Residual of one interior cell and the stage combination.  The state update runs in
+// FP64 for both precision forms.  FP64 path: qin/qout are double stage states as in
+// integrators.d.  Split path: qin is the FP32 stage input, q64 is updated in FP64 and
+// the next stage input (qout) is its FP32 rounding.
+template <typename T, int ST>
+__global__ void __launch_bounds__(UPD_THREADS) k_update(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, T *qout,
+                                                       int dt_update, int need_dt, int final_stage)
+{
+    constexpr bool SPLIT = sizeof(T) == 4;
+    DState *st = A.st;
+    if (halted(st)) return;
+    __shared__ double sh[UPD_THREADS / 32][10];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool act = i < M.C;
+    double dtc = INFINITY, rm = 0.0;
+    double ss[4] = {0, 0, 0, 0}, vs[4] = {0, 0, 0, 0};
+    bool bad = false;
+    if (act) {
+        const int Cs = M.Cs;
+        const int ne = M.nedge[i];
+        const T *fl = reinterpret_cast<const T *>(A.fl);
+        const T *fs = reinterpret_cast<const T *>(A.fs);
+        T r[4] = {T(0.0), T(0.0), T(0.0), T(0.0)};
+        T sAve = 0;
+        for (int j = 0; j < ne; j++) {
+            const int ev = M.s_edge[(size_t)j * Cs + i];
+            const size_t e = (size_t)(ev & 0x7fffffff);
+            T f[4];
+            ld4(fl + 4 * e, f);
+            if (ev < 0) {
+#pragma unroll
+                for (int k = 0; k < 4; k++) r[k] = r[k] + (-f[k]);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; k++) r[k] = r[k] + f[k];
+            }
+            sAve += fs[e];
+        }
+        T *cdt = reinterpret_cast<T *>(A.cdt);
+        if (need_dt || (P.local_ts && dt_update)) {
+            sAve /= ld1<T>(M.g.perim, i);
+            T c = ((T)st->cfl * ld1<T>(M.g.dlen, i)) / sAve;
+            if (need_dt) dtc = (double)c;
+            if (P.local_ts && dt_update) cdt[i] = isnan(c) ? T(0.0) : c;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            if ((double)fabs(r[k]) > rm) rm = (double)fabs(r[k]);
+        const T s = ld1<T>(M.g.neg_inv_area, i);
+        T R[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) R[k] = r[k] * s;
+        if (P.mms) {
+            T S[4];
+            ld4(ptr<T>(M.g.src) + 4 * (size_t)i, S);
+#pragma unroll
+            for (int k = 0; k < 4; k++) R[k] = R[k] + S[k];
+        }
+        if (ST == ST_RESID) {
+            st4(reinterpret_cast<T *>(A.R) + 4 * (size_t)i, R);
+        } else {
+            T *aux = reinterpret_cast<T *>(A.aux);
+            double q0[4], Rd[4], out[4];
+            ld4(A.q64 + 4 * (size_t)i, q0);
+#pragma unroll
+            for (int k = 0; k < 4; k++) Rd[k] = (double)R[k];
+            const double dt = st->dt;
+            const double h = P.local_ts ? (double)cdt[i] : dt;
+            if (ST == ST_EULER) {
+#pragma unroll
+                for (int k = 0; k < 4; k++) out[k] = q0[k] + h * Rd[k];
+            } else if (ST == ST_RK2_1) {
+                st4(aux + 4 * (size_t)i, R);
+#pragma unroll
+                for (int k = 0; k < 4; k++) out[k] = q0[k] + (dt * Rd[k]);
+            } else if (ST == ST_RK2_2) {
+                T k1[4];
+                ld4(aux + 4 * (size_t)i, k1);
+                const double hh = P.local_ts ? h / 2.0 : st->dt_half;
+                if (SPLIT) {
+#pragma unroll
+                    for (int k = 0; k < 4; k++) out[k] = q0[k] + hh * ((double)k1[k] + Rd[k]);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 4; k++) out[k] = q0[k] + hh * (k1[k] + R[k]);
+                }
+            } else if (ST == ST_TVD_1) {
+                if (SPLIT) st4(aux + 4 * (size_t)i, R);
+#pragma unroll
+                for (int k = 0; k < 4; k++) out[k] = q0[k] + h * Rd[k];
+            } else if (ST == ST_TVD_2) {
+                double qfe[4];
+                if (SPLIT) {  // recompute qFE = q + h R1 in FP64 from the FP32 R1
+                    T r1[4];
+                    ld4(aux + 4 * (size_t)i, r1);
+#pragma unroll
+                    for (int k = 0; k < 4; k++) qfe[k] = q0[k] + h * (double)r1[k];
+                } else {
+                    ld4(reinterpret_cast<const double *>(qin) + 4 * (size_t)i, qfe);
+                }
+#pragma unroll
+                for (int k = 0; k < 4; k++) out[k] = 0.5 * (q0[k] + qfe[k] + h * Rd[k]);
+            } else if (ST == ST_RK4_1) {
+                st4(aux + 4 * (size_t)i, R);
+#pragma unroll
+                for (int k = 0; k < 4; k++) out[k] = q0[k] + (st->dt_half * Rd[k]);
+            } else if (ST == ST_RK4_2 || ST == ST_RK4_3) {
+                T acc[4];
+                ld4(aux + 4 * (size_t)i, acc);
+#pragma unroll
+                for (int k = 0; k < 4; k++) acc[k] = acc[k] + T(2.0) * R[k];
+                st4(aux + 4 * (size_t)i, acc);
+                if (ST == ST_RK4_2) {
+#pragma unroll
+                    for (int k = 0; k < 4; k++) out[k] = q0[k] + (st->dt_half * Rd[k]);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 4; k++) out[k] = q0[k] + (dt * Rd[k]);
+                }
+            } else {  // ST_RK4_4
+                T acc[4];
+                ld4(aux + 4 * (size_t)i, acc);
+                const double hh = P.local_ts ? h / 6.0 : st->dt_sixth;
+                if (SPLIT) {
+#pragma unroll
+                    for (int k = 0; k < 4; k++) out[k] = q0[k] + hh * ((double)acc[k] + Rd[k]);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 4; k++) out[k] = q0[k] + hh * (acc[k] + R[k]);
+                }
+            }
+            if (final_stage) {
+                st4(A.q64 + 4 * (size_t)i, out);
+                if (SPLIT) {
+                    T o[4] = {(T)out[0], (T)out[1], (T)out[2], (T)out[3]};
+                    st4(qout + 4 * (size_t)i, o);
+                }
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    double d = out[k] - q0[k];
+                    ss[k] = d * d;
+                    vs[k] = out[k];
+                }
+                bad = isnan(out[0]) || isnan(out[1]) || isnan(out[2]) || isnan(out[3]);
+            } else {
+                T o[4] = {(T)out[0], (T)out[1], (T)out[2], (T)out[3]};
+                st4(qout + 4 * (size_t)i, o);
+            }
+        }
+    }
+    if (bad) flag_error(st, 3, ERR_NAN_CELL, (unsigned)M.cell_ref[i]);
+    // block reductions: dt (min), Rmax (max), RMS partials (sum) in a fixed tree
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    dtc = warp_min(dtc);
+    rm = warp_max(rm);
+    if (final_stage) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            ss[k] = warp_sum(ss[k]);
+            vs[k] = warp_sum(vs[k]);
+        }
+    }
+    if (lane == 0) {
+        sh[w][0] = dtc;
+        sh[w][1] = rm;
+        for (int k = 0; k < 4; k++) {
+            sh[w][2 + k] = ss[k];
+            sh[w][6 + k] = vs[k];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = sh[0][0], b = sh[0][1];
+        double s8[8];
+        for (int k = 0; k < 8; k++) s8[k] = sh[0][2 + k];
+        for (int ww = 1; ww < UPD_THREADS / 32; ww++) {
+            a = fmin(a, sh[ww][0]);
+            b = fmax(b, sh[ww][1]);
+            for (int k = 0; k < 8; k++) s8[k] = s8[k] + sh[ww][2 + k];
+        }
+        if (need_dt && a == a) atomicMin(&st->newdt_bits, (unsigned long long)__double_as_longlong(a));
+        if (b > 0) atomicMax(&st->rmax_bits, (unsigned long long)__double_as_longlong(b));
+        if (final_stage)
+            for (int k = 0; k < 8; k++) A.red[8 * (size_t)blockIdx.x + k] = s8[k];
+    }
+}
+
+inline int ret(cudaError_t e) { return e == cudaSuccess ? 0 : (int)e; }
+
+template <typename T>
+int launch_cell_impl(const DMesh &M, const DPhys &P, const DArrays &A, const T *qin, int limit, void *stream)
+{
+    const int TB = 128;
+    dim3 grid((M.C + TB - 1) / TB);
+    if (grid.x == 0) return 0;
+    cudaStream_t s = (cudaStream_t)stream;
+    const bool lp = P.lp && P.limited;
+#define EBB_CELL(MJ)                                                          \
+    if (lp)                                                                   \
+        k_cell<T, MJ, true><<<grid, TB, 0, s>>>(M, P, A, qin, limit);         \
+    else                                                                      \
+        k_cell<T, MJ, false><<<grid, TB, 0, s>>>(M, P, A, qin, limit);
+    if (M.maxJ <= 3) {
+        EBB_CELL(3)
+    } else if (M.maxJ == 4) {
+        EBB_CELL(4)
+    } else {
+        EBB_CELL(6)
+    }
+#undef EBB_CELL
+    return ret(cudaGetLastError());
+}
+
+template <typename T> int launch_flux_impl(const DMesh &M, const DPhys &P, const DArrays &A, const T *qin, void *stream)
+{
+    const int TB = 128;
+    int nbi = (M.Eint + TB - 1) / TB, nbb = (M.G + TB - 1) / TB;
+    if (nbi + nbb == 0) return 0;
+    k_flux<T><<<nbi + nbb, TB, 0, (cudaStream_t)stream>>>(M, P, A, qin, nbi);
+    return ret(cudaGetLastError());
+}
+
+template <typename T>
+int launch_update_impl(const DMesh &M, const DPhys &P, const DArrays &A, int stage, const T *qin, T *qout,
+                       int dt_update, int need_dt, int final_stage, void *stream)
+{
+    dim3 grid((M.C + UPD_THREADS - 1) / UPD_THREADS);
+    if (grid.x == 0) return 0;
+    cudaStream_t s = (cudaStream_t)stream;
+#define EBB_UPD(S)                                                                                       \
+    case S:                                                                                              \
+        k_update<T, S><<<grid, UPD_THREADS, 0, s>>>(M, P, A, qin, qout, dt_update, need_dt, final_stage); \
+        break;
+    switch (stage) {
+        EBB_UPD(ST_RESID)
+        EBB_UPD(ST_EULER)
+        EBB_UPD(ST_RK2_1)
+        EBB_UPD(ST_RK2_2)
+        EBB_UPD(ST_TVD_1)
+        EBB_UPD(ST_TVD_2)
+        EBB_UPD(ST_RK4_1)
+        EBB_UPD(ST_RK4_2)
+        EBB_UPD(ST_RK4_3)
+        EBB_UPD(ST_RK4_4)
+    default:
+        return -1;
+    }
+#undef EBB_UPD
+    return ret(cudaGetLastError());
+}
+
+}  // namespace ebbdev
+
+#define EBB_INSTANTIATE(T)                                                                                        \
+    template <>                                                                                                   \
+    int launch_cell<T>(const DMesh &M, const DPhys &P, const DArrays &A, const T *qin, int limit, void *stream)  \
+    {                                                                                                             \
+        return ebbdev::launch_cell_impl<T>(M, P, A, qin, limit, stream);                                          \
+    }                                                                                                             \
+    template <>                                                                                                   \
+    int launch_flux<T>(const DMesh &M, const DPhys &P, const DArrays &A, const T *qin, void *stream)              \
+    {                                                                                                             \
+        return ebbdev::launch_flux_impl<T>(M, P, A, qin, stream);                                                 \
+    }                                                                                                             \
+    template <>                                                                                                   \
+    int launch_update<T>(const DMesh &M, const DPhys &P, const DArrays &A, int stage, const T *qin, T *qout,      \
+                         int dt_update, int need_dt, int final_stage, void *stream)                               \
+    {                                                                                                             \
+        return ebbdev::launch_update_impl<T>(M, P, A, stage, qin, qout, dt_update, need_dt, final_stage, stream); \
+    }

@@ -2,14 +2,17 @@
 //
 // HBM layout (C interior cells in RCM order, G ghost cells = boundary edges ordered by
 // owner, Eint interior edges sorted by first cell, Cs = C rounded up to 32):
-//   state   q, qs, aux           double[4] per cell (32 B, one sector), ghosts at [C, C+G)
+//   state   q64 double[4] per cell (32 B, one sector) = the solution; stage inputs qs1/qs
+//           in the arithmetic type T (double: qs1 aliases q64; float: a float[4] shadow),
+//           ghosts at [C, C+G)
 //   slots   ELL, slot (i, j) at j*Cs + i, j < nedge[i] in the reference's local edge order:
-//           nbr int32, edge int32 (bit 31 = fluxMultiplier -1), gm double[2] (gradMat
-//           column), nd double[2] (neighbour centroid - centroid), fd double[2] (edge
-//           midpoint - centroid), face double[4] (reconstructed face state)
-//   edges   slot int32[2], cell int32[2], n double[2], len double; fluxes fl double[4]
-//           (len*F) and fs double (len*sMax) for interior edges then boundary edges
-//   cells   nedge int32, neg_inv_area, perim, d, src double[4] (manufactured source)
+//           nbr int32, edge int32 (bit 31 = fluxMultiplier -1), gm T[2] (gradMat column),
+//           nd T[2] (neighbour centroid - centroid), fd T[2] (edge midpoint - centroid),
+//           face T[4] (reconstructed face state)
+//   edges   slot int32[2], cell int32[2], n T[2], len T; fluxes fl T[4] (len*F) and fs T
+//           (len*sMax) for interior edges then boundary edges
+//   cells   nedge int32, neg_inv_area, perim, d, src T[4] (manufactured source)
+// All geometry is computed on the host in FP64; the split path stores FP32 copies.
 #pragma once
 #include <stdint.h>
 
@@ -17,23 +20,27 @@
 #define EBB_REC_CAP 4096
 #define EBB_RED_THREADS 256
 
+// real-valued mesh arrays, in the arithmetic type of a precision form
+struct DGeo {
+    const void *s_gm, *s_nd, *s_fd;             // T[2] per slot
+    const void *neg_inv_area, *perim, *dlen;     // T per cell
+    const void *src;                             // T[4] per cell or null
+    const void *e_n, *e_len;                     // T[2], T per interior edge
+    const void *b_n, *b_len;                     // T[2], T per boundary edge
+    const void *b_refl, *b_data, *b_dq, *b_dmid; // T[4] per boundary edge
+};
+
 struct DMesh {
     int32_t C, G, Cs, Eint, maxJ;
     const int32_t *nedge;
     const int32_t *s_nbr, *s_edge;
-    const double *s_gm, *s_nd, *s_fd;  // double2 per slot
-    const double *neg_inv_area, *perim, *dlen, *src;  // src: double4 per cell or null
     const int32_t *e_slot, *e_cell;    // int2 per interior edge
-    const double *e_n, *e_len;         // double2, double
     const int32_t *b_cell, *b_slot, *b_type;
-    const double *b_n, *b_len;         // double2, double
-    const double *b_refl;              // double4: reflection matrix (r00, r01, r10, r11)
-    const double *b_data;              // double4: FullState q_inf | ConstP pb | TPInflow Tt, Pt, nin0, nin1
-    const double *b_dq, *b_dmid;       // double4: Dirichlet state at ghost centroid / edge midpoint
     const int32_t *e_ref, *b_ref;      // reference edge ids (error reports)
     const int32_t *cell_ref;           // reference cell id per device cell
     const int32_t *force_b;            // boundary indices summed for forces
     int32_t n_force;
+    DGeo g;                            // arrays in the kernels' arithmetic type
 };
 
 struct DPhys {
@@ -79,30 +86,42 @@ enum StageKind {
 };
 
 struct DArrays {
-    double *q, *qs, *aux, *face, *grad, *fl, *fs, *cdt, *R;
-    double *red;  // per-block partial sums (8 per block)
+    double *q64;          // solution, FP64, C (+G) x 4
+    void *qs1;            // stage-1 input in T (FP64 path: == q64)
+    void *qs;             // later-stage input in T
+    void *aux;            // k1 / R1 / RK4 accumulator in T
+    void *face, *grad, *fl, *fs, *cdt, *R;
+    double *red;          // per-block partial sums (8 per block)
     DState *st;
     DRecord *rec;
 };
 
 #ifdef __cplusplus
 extern "C++" {
-// launch wrappers (k_fp64.cu)
-int launch_cell_fp64(const DMesh &M, const DPhys &P, const DArrays &A, const double *qin, double *qin_ghost_out,
-                     int limit, void *stream);
-int launch_flux_fp64(const DMesh &M, const DPhys &P, const DArrays &A, const double *qin, void *stream);
-int launch_update_fp64(const DMesh &M, const DPhys &P, const DArrays &A, int stage, const double *qin, double *qout,
-                       int dt_update, int need_dt, int final_stage, void *stream);
-int launch_step_end(const DMesh &M, const DArrays &A, int nred_blocks, void *stream);
+// launch wrappers; T = double (k_fp64.cu) or float (k_split.cu)
+template <typename T>
+int launch_cell(const DMesh &M, const DPhys &P, const DArrays &A, const T *qin, int limit, void *stream);
+template <typename T> int launch_flux(const DMesh &M, const DPhys &P, const DArrays &A, const T *qin, void *stream);
+template <typename T>
+int launch_update(const DMesh &M, const DPhys &P, const DArrays &A, int stage, const T *qin, T *qout, int dt_update,
+                  int need_dt, int final_stage, void *stream);
+template <> int launch_cell<double>(const DMesh &, const DPhys &, const DArrays &, const double *, int, void *);
+template <> int launch_cell<float>(const DMesh &, const DPhys &, const DArrays &, const float *, int, void *);
+template <> int launch_flux<double>(const DMesh &, const DPhys &, const DArrays &, const double *, void *);
+template <> int launch_flux<float>(const DMesh &, const DPhys &, const DArrays &, const float *, void *);
+template <>
+int launch_update<double>(const DMesh &, const DPhys &, const DArrays &, int, const double *, double *, int, int, int,
+                          void *);
+template <>
+int launch_update<float>(const DMesh &, const DPhys &, const DArrays &, int, const float *, float *, int, int, int,
+                         void *);
+int launch_step_end(const DMesh &M, const DArrays &A, int nred_blocks, int split, void *stream);
 int launch_flux_batch(int kind, int64_t n, const double *qL, const double *qR, const double *nrm, double *F,
                       double *s, void *stream);
 int update_blocks(int C);
-}
-#endif
-
-#ifdef __cplusplus
-extern "C++" {
-// reference-order <-> device-order state copies (k_fp64.cu)
+// reference-order <-> device-order state copies; conversions for the split path
 int launch_permute4(const double *src, double *dst, const int32_t *idx, int64_t n, int gather, void *stream);
+int launch_to_float4(const double *src, float *dst, int64_t n, void *stream);
+int launch_to_double4(const float *src, double *dst, int64_t n, void *stream);
 }
 #endif

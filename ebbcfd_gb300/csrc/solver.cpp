@@ -73,39 +73,40 @@ void freestream(double M, double aoa_deg, double rho, double q[4])
     q[3] = p / (1.4 - 1.0) + 0.5 * rho * (u * u + v * v);
 }
 
-int run_stage(ebb_solver *s, int stage, double *qin, double *qout, int limit, int dt_update, int need_dt, int final_stage)
+template <typename T>
+int run_stage_t(ebb_solver *s, int stage, T *qin, T *qout, int limit, int dt_update, int need_dt, int final_stage)
 {
-    CKL(launch_cell_fp64(s->M, s->P, s->A, qin, qin, limit, s->stream));
-    CKL(launch_flux_fp64(s->M, s->P, s->A, qin, s->stream));
-    CKL(launch_update_fp64(s->M, s->P, s->A, stage, qin, qout, dt_update, need_dt, final_stage, s->stream));
+    CKL(launch_cell<T>(s->M, s->P, s->A, qin, limit, s->stream));
+    CKL(launch_flux<T>(s->M, s->P, s->A, qin, s->stream));
+    CKL(launch_update<T>(s->M, s->P, s->A, stage, qin, qout, dt_update, need_dt, final_stage, s->stream));
     return EBB_OK;
 }
 
-// integrators.d: stage sequence of one step on the resident state A.q
-int integrator_stages(ebb_solver *s)
+// integrators.d: stage sequence of one step on the resident state
+template <typename T> int integrator_stages_t(ebb_solver *s)
 {
     const ebb_config &c = s->cfg;
-    double *q = s->A.q, *qs = s->A.qs;
+    T *q1 = reinterpret_cast<T *>(s->A.qs1), *qs = reinterpret_cast<T *>(s->A.qs);
     const int ms = c.multistage_limiting;
     const int lts = c.local_timestep;
     int r = EBB_OK;
     switch (c.integrator) {
     case EBB_INT_EULER:
-        r = run_stage(s, ST_EULER, q, q, 1, 1, 1, 1);
+        r = run_stage_t<T>(s, ST_EULER, q1, q1, 1, 1, 1, 1);
         break;
     case EBB_INT_RK2:
-        if ((r = run_stage(s, ST_RK2_1, q, qs, 1, 1, 0, 0))) break;
-        r = run_stage(s, ST_RK2_2, qs, q, ms, 0, 1, 1);
+        if ((r = run_stage_t<T>(s, ST_RK2_1, q1, qs, 1, 1, 0, 0))) break;
+        r = run_stage_t<T>(s, ST_RK2_2, qs, q1, ms, 0, 1, 1);
         break;
     case EBB_INT_RK2_TVD:
-        if ((r = run_stage(s, ST_TVD_1, q, qs, 1, lts, 0, 0))) break;
-        r = run_stage(s, ST_TVD_2, qs, q, 0, !lts, 1, 1);
+        if ((r = run_stage_t<T>(s, ST_TVD_1, q1, qs, 1, lts, 0, 0))) break;
+        r = run_stage_t<T>(s, ST_TVD_2, qs, q1, 0, !lts, 1, 1);
         break;
     case EBB_INT_RK4:
-        if ((r = run_stage(s, ST_RK4_1, q, qs, 1, 1, 0, 0))) break;
-        if ((r = run_stage(s, ST_RK4_2, qs, qs, ms, 0, 0, 0))) break;
-        if ((r = run_stage(s, ST_RK4_3, qs, qs, ms, 0, 0, 0))) break;
-        r = run_stage(s, ST_RK4_4, qs, q, ms, 0, 1, 1);
+        if ((r = run_stage_t<T>(s, ST_RK4_1, q1, qs, 1, 1, 0, 0))) break;
+        if ((r = run_stage_t<T>(s, ST_RK4_2, qs, qs, ms, 0, 0, 0))) break;
+        if ((r = run_stage_t<T>(s, ST_RK4_3, qs, qs, ms, 0, 0, 0))) break;
+        r = run_stage_t<T>(s, ST_RK4_4, qs, q1, ms, 0, 1, 1);
         break;
     default:
         r = fail(s, EBB_ERR_CONFIG, "unknown integrator");
@@ -113,12 +114,28 @@ int integrator_stages(ebb_solver *s)
     return r;
 }
 
+int integrator_stages(ebb_solver *s)
+{
+    return s->precision == EBB_PREC_SPLIT ? integrator_stages_t<float>(s) : integrator_stages_t<double>(s);
+}
+
 int one_loop_step(ebb_solver *s)
 {
     int r = integrator_stages(s);
     if (r) return r;
-    CKL(launch_step_end(s->M, s->A, s->nred, s->stream));
+    CKL(launch_step_end(s->M, s->A, s->nred, s->precision == EBB_PREC_SPLIT, s->stream));
     return EBB_OK;
+}
+
+// stage kernels of one residual evaluation on the stage buffer qs (ST_RESID writes R)
+int residual_kernels(ebb_solver *s, int limit, int dt_update)
+{
+    if (s->precision == EBB_PREC_SPLIT) {
+        float *qs = reinterpret_cast<float *>(s->A.qs);
+        return run_stage_t<float>(s, ST_RESID, qs, nullptr, limit, dt_update, 1, 0);
+    }
+    double *qs = reinterpret_cast<double *>(s->A.qs);
+    return run_stage_t<double>(s, ST_RESID, qs, nullptr, limit, dt_update, 1, 0);
 }
 
 int build_graph(ebb_solver *s, int steps, cudaGraphExec_t *out)
@@ -171,6 +188,36 @@ int solver_write_state(ebb_solver *s, const DState &h)
 
 }  // namespace ebb
 
+template <typename T> int profile_t(ebb_solver *s, int32_t n_rep, double *ms)
+{
+    // work on a copy of the stage-1 state so the resident solution is untouched
+    const size_t bytes = sizeof(T) * 4 * (size_t)(s->C + s->G);
+    CK(cudaMemcpyAsync(s->A.qs, s->A.qs1, bytes, cudaMemcpyDeviceToDevice, s->stream));
+    T *qs = reinterpret_cast<T *>(s->A.qs);
+    T *scratch = reinterpret_cast<T *>(s->A.face);  // update output target (rebuilt below)
+    cudaEvent_t ev[2];
+    CK(cudaEventCreate(&ev[0]));
+    CK(cudaEventCreate(&ev[1]));
+    for (int k = 0; k < 4; k++) {
+        float t = 0;
+        CK(cudaEventRecord(ev[0], s->stream));
+        for (int i = 0; i < n_rep; i++) {
+            if (k == 0) CKL(launch_cell<T>(s->M, s->P, s->A, qs, 1, s->stream));
+            if (k == 1) CKL(launch_flux<T>(s->M, s->P, s->A, qs, s->stream));
+            if (k == 2) CKL(launch_update<T>(s->M, s->P, s->A, ST_RK2_1, qs, scratch, 1, 1, 0, s->stream));
+            if (k == 3) CKL(launch_step_end(s->M, s->A, s->nred, sizeof(T) == 4, s->stream));
+        }
+        CK(cudaEventRecord(ev[1], s->stream));
+        CK(cudaEventSynchronize(ev[1]));
+        CK(cudaEventElapsedTime(&t, ev[0], ev[1]));
+        ms[k] = (double)t / n_rep;
+        if (k == 2) CKL(launch_cell<T>(s->M, s->P, s->A, qs, 1, s->stream));
+    }
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    return EBB_OK;
+}
+
 extern "C" {
 
 int ebb_abi_version(void) { return EBB_ABI_VERSION; }
@@ -209,8 +256,8 @@ int ebb_solver_create(const ebb_mesh *mesh, const ebb_config *cfg, int32_t preci
 {
     if (!mesh || !cfg || !out) return EBB_ERR_ARG;
     *out = nullptr;
-    if (precision != EBB_PREC_FP64) {
-        set_err(err, err_len, "precision form not available in this build");
+    if (precision != EBB_PREC_FP64 && precision != EBB_PREC_SPLIT) {
+        set_err(err, err_len, "unknown precision form");
         return EBB_ERR_ARG;
     }
     int ndev = 0;
@@ -450,22 +497,24 @@ int ebb_solver_create(const ebb_mesh *mesh, const ebb_config *cfg, int32_t preci
     }
 
     // ---- device allocation (one arena) ----------------------------------------
+    const bool split = precision == EBB_PREC_SPLIT;
+    const size_t rs = split ? sizeof(float) : sizeof(double);  // bytes of the arithmetic type
     const int64_t NQ = C + G;
     s->nred = update_blocks((int)C);
+    auto rsz = [&](size_t n) { return ((n * rs) + 255) & ~(size_t)255; };
     size_t total = 0;
-    total += 3 * sz<double>(4 * NQ);                    // q, qs, aux
-    total += sz<double>(4 * MJ * Cs);                   // face
-    total += sz<double>(8 * NQ);                        // grad
-    total += sz<double>(4 * (Eint + G)) + sz<double>(Eint + G);  // fl, fs
-    total += sz<double>(C);                             // cdt
-    total += sz<double>(8 * (size_t)s->nred);           // red
-    total += sz<DState>(1) + sz<DRecord>(EBB_REC_CAP);
-    total += sz<int32_t>(C) * 3 + sz<double>(C) * 3 + (cfg->mms ? sz<double>(4 * C) : 0);
-    total += 2 * sz<int32_t>(MJ * Cs) + 3 * sz<double>(2 * MJ * Cs);
-    total += 2 * sz<int32_t>(2 * Eint) + sz<double>(2 * Eint) + sz<double>(Eint) + sz<int32_t>(Eint);
-    total += 4 * sz<int32_t>(G) + sz<double>(2 * G) + sz<double>(G) + 4 * sz<double>(4 * G);
+    total += sz<double>(4 * NQ);                                        // q64
+    total += split ? rsz(4 * NQ) : 0;                                   // qs1 (float shadow)
+    total += 2 * rsz(4 * NQ);                                           // qs, aux
+    total += rsz(4 * MJ * Cs) + rsz(8 * NQ);                            // face, grad
+    total += rsz(4 * (Eint + G)) + rsz(Eint + G) + rsz(C);              // fl, fs, cdt
+    total += sz<double>(8 * (size_t)s->nred) + sz<DState>(1) + sz<DRecord>(EBB_REC_CAP);
+    total += 3 * sz<int32_t>(C) + 3 * rsz(C) + (cfg->mms ? rsz(4 * C) : 0);
+    total += 2 * sz<int32_t>(MJ * Cs) + 3 * rsz(2 * MJ * Cs);
+    total += 2 * sz<int32_t>(2 * Eint) + rsz(2 * Eint) + rsz(Eint) + sz<int32_t>(Eint);
+    total += 4 * sz<int32_t>(G) + rsz(2 * G) + rsz(G) + 4 * rsz(4 * G);
     total += sz<int32_t>(h_force.size() + 1);
-    total += sz<double>(4 * C);  // staging
+    total += 2 * sz<double>(4 * C);  // host-order staging, device-order scratch
     s->dbytes = total;
     cudaError_t ce = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
     if (ce == cudaSuccess) ce = cudaMalloc(&s->dmem, total);
@@ -478,14 +527,16 @@ int ebb_solver_create(const ebb_mesh *mesh, const ebb_config *cfg, int32_t preci
     cudaMemsetAsync(s->dmem, 0, total, s->stream);
     Arena ar{(char *)s->dmem, 0, total};
     DArrays &A = s->A;
-    A.q = ar.take<double>(4 * NQ);
-    A.qs = ar.take<double>(4 * NQ);
-    A.aux = ar.take<double>(4 * NQ);
-    A.face = ar.take<double>(4 * MJ * Cs);
-    A.grad = ar.take<double>(8 * NQ);
-    A.fl = ar.take<double>(4 * (Eint + G));
-    A.fs = ar.take<double>(Eint + G);
-    A.cdt = ar.take<double>(C);
+    auto takeR = [&](size_t n) -> void * { return split ? (void *)ar.take<float>(n) : (void *)ar.take<double>(n); };
+    A.q64 = ar.take<double>(4 * NQ);
+    A.qs1 = split ? takeR(4 * NQ) : (void *)A.q64;
+    A.qs = takeR(4 * NQ);
+    A.aux = takeR(4 * NQ);
+    A.face = takeR(4 * MJ * Cs);
+    A.grad = takeR(8 * NQ);
+    A.fl = takeR(4 * (Eint + G));
+    A.fs = takeR(Eint + G);
+    A.cdt = takeR(C);
     A.red = ar.take<double>(8 * (size_t)s->nred);
     A.st = ar.take<DState>(1);
     A.rec = ar.take<DRecord>(EBB_REC_CAP);
@@ -500,45 +551,43 @@ int ebb_solver_create(const ebb_mesh *mesh, const ebb_config *cfg, int32_t preci
         if (!v.empty()) cudaMemcpyAsync((void *)dst, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice, s->stream);
         return dst;
     };
+    // real arrays: FP64 precompute, stored in the arithmetic type
+    auto upR = [&](const std::vector<double> &v) -> const void * {
+        void *dst = takeR(v.size() ? v.size() : 1);
+        if (v.empty()) return dst;
+        if (split) {
+            std::vector<float> f(v.begin(), v.end());
+            cudaMemcpyAsync(dst, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream);
+            cudaStreamSynchronize(s->stream);
+        } else {
+            cudaMemcpyAsync(dst, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, s->stream);
+        }
+        return dst;
+    };
     int32_t *p_nedge = ar.take<int32_t>(C);
-    up(p_nedge, h_nedge);
-    M.nedge = p_nedge;
+    M.nedge = up(p_nedge, h_nedge);
     int32_t *p_cellref = ar.take<int32_t>(C);
-    up(p_cellref, h_cellref);
-    M.cell_ref = p_cellref;
+    M.cell_ref = up(p_cellref, h_cellref);
     s->d_perm = ar.take<int32_t>(C);
     up(s->d_perm, h_cellref);
-    double *p;
-    p = ar.take<double>(C);
-    M.neg_inv_area = up(p, h_nia);
-    p = ar.take<double>(C);
-    M.perim = up(p, h_perim);
-    p = ar.take<double>(C);
-    M.dlen = up(p, h_d);
-    M.src = nullptr;
-    if (cfg->mms) {
-        p = ar.take<double>(4 * C);
-        M.src = up(p, h_src);
-    }
+    M.g.neg_inv_area = upR(h_nia);
+    M.g.perim = upR(h_perim);
+    M.g.dlen = upR(h_d);
+    M.g.src = cfg->mms ? upR(h_src) : nullptr;
     int32_t *pi;
     pi = ar.take<int32_t>(MJ * Cs);
     M.s_nbr = up(pi, h_snbr);
     pi = ar.take<int32_t>(MJ * Cs);
     M.s_edge = up(pi, h_sedge);
-    p = ar.take<double>(2 * MJ * Cs);
-    M.s_gm = up(p, h_sgm);
-    p = ar.take<double>(2 * MJ * Cs);
-    M.s_nd = up(p, h_snd);
-    p = ar.take<double>(2 * MJ * Cs);
-    M.s_fd = up(p, h_sfd);
+    M.g.s_gm = upR(h_sgm);
+    M.g.s_nd = upR(h_snd);
+    M.g.s_fd = upR(h_sfd);
     pi = ar.take<int32_t>(2 * Eint);
     M.e_slot = up(pi, h_eslot);
     pi = ar.take<int32_t>(2 * Eint);
     M.e_cell = up(pi, h_ecell);
-    p = ar.take<double>(2 * Eint);
-    M.e_n = up(p, h_en);
-    p = ar.take<double>(Eint);
-    M.e_len = up(p, h_elen);
+    M.g.e_n = upR(h_en);
+    M.g.e_len = upR(h_elen);
     pi = ar.take<int32_t>(Eint);
     M.e_ref = up(pi, h_eref);
     pi = ar.take<int32_t>(G);
@@ -549,24 +598,26 @@ int ebb_solver_create(const ebb_mesh *mesh, const ebb_config *cfg, int32_t preci
     M.b_type = up(pi, h_btype);
     pi = ar.take<int32_t>(G);
     M.b_ref = up(pi, h_bref);
-    p = ar.take<double>(2 * G);
-    M.b_n = up(p, h_bn);
-    p = ar.take<double>(G);
-    M.b_len = up(p, h_blen);
-    p = ar.take<double>(4 * G);
-    M.b_refl = up(p, h_brefl);
-    p = ar.take<double>(4 * G);
-    M.b_data = up(p, h_bdata);
-    p = ar.take<double>(4 * G);
-    M.b_dq = up(p, h_bdq);
-    p = ar.take<double>(4 * G);
-    M.b_dmid = up(p, h_bdmid);
+    M.g.b_n = upR(h_bn);
+    M.g.b_len = upR(h_blen);
+    M.g.b_refl = upR(h_brefl);
+    M.g.b_data = upR(h_bdata);
+    M.g.b_dq = upR(h_bdq);
+    M.g.b_dmid = upR(h_bdmid);
     pi = ar.take<int32_t>(h_force.size() + 1);
     M.force_b = up(pi, h_force);
     M.n_force = (int32_t)h_force.size();
     s->d_stage = ar.take<double>(4 * C);
-    up(A.q, h_q);
-    up(A.grad, h_grad);
+    s->d_tmp = ar.take<double>(4 * C);
+    up(A.q64, h_q);
+    if (split) {
+        std::vector<float> gf(h_grad.begin(), h_grad.end());
+        cudaMemcpyAsync(A.grad, gf.data(), gf.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream);
+        cudaStreamSynchronize(s->stream);
+        launch_to_float4(A.q64, reinterpret_cast<float *>(A.qs1), C, s->stream);
+    } else {
+        up(reinterpret_cast<double *>(A.grad), h_grad);
+    }
 
     DPhys &P = s->P;
     P.flux = cfg->flux;
@@ -640,7 +691,9 @@ int ebb_set_state(ebb_solver *s, const double *q)
 {
     if (!s || !q) return EBB_ERR_ARG;
     CK(cudaMemcpyAsync(s->d_stage, q, sizeof(double) * 4 * s->C, cudaMemcpyHostToDevice, s->stream));
-    CKL(launch_permute4(s->d_stage, s->A.q, s->d_perm, s->C, 1, s->stream));
+    CKL(launch_permute4(s->d_stage, s->A.q64, s->d_perm, s->C, 1, s->stream));
+    if (s->precision == EBB_PREC_SPLIT)
+        CKL(launch_to_float4(s->A.q64, reinterpret_cast<float *>(s->A.qs1), s->C, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     return EBB_OK;
 }
@@ -648,7 +701,7 @@ int ebb_set_state(ebb_solver *s, const double *q)
 int ebb_get_state(ebb_solver *s, double *q)
 {
     if (!s || !q) return EBB_ERR_ARG;
-    CKL(launch_permute4(s->A.q, s->d_stage, s->d_perm, s->C, 0, s->stream));
+    CKL(launch_permute4(s->A.q64, s->d_stage, s->d_perm, s->C, 0, s->stream));
     CK(cudaMemcpyAsync(q, s->d_stage, sizeof(double) * 4 * s->C, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     return EBB_OK;
@@ -685,10 +738,8 @@ int ebb_residual(ebb_solver *s, const double *q, double *R, double *new_dt, doub
 {
     if (!s || !q || !R) return EBB_ERR_ARG;
     CK(cudaMemcpyAsync(s->d_stage, q, sizeof(double) * 4 * s->C, cudaMemcpyHostToDevice, s->stream));
-    CKL(launch_permute4(s->d_stage, s->A.qs, s->d_perm, s->C, 1, s->stream));
-    int r = solver_run_residual_on_qs(s, limit, dt_update, new_dt, rmax);
+    int r = ebb_residual_device(s, s->d_stage, s->d_stage, new_dt, rmax, limit, dt_update);
     if (r) return r;
-    CKL(launch_permute4(s->A.R, s->d_stage, s->d_perm, s->C, 0, s->stream));
     CK(cudaMemcpyAsync(R, s->d_stage, sizeof(double) * 4 * s->C, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     return EBB_OK;
@@ -698,10 +749,21 @@ int ebb_residual_device(ebb_solver *s, const double *q_dev, double *R_dev, doubl
                         int32_t dt_update)
 {
     if (!s || !q_dev || !R_dev) return EBB_ERR_ARG;
-    CKL(launch_permute4(q_dev, s->A.qs, s->d_perm, s->C, 1, s->stream));
+    const bool split = s->precision == EBB_PREC_SPLIT;
+    if (split) {
+        CKL(launch_permute4(q_dev, s->d_tmp, s->d_perm, s->C, 1, s->stream));
+        CKL(launch_to_float4(s->d_tmp, reinterpret_cast<float *>(s->A.qs), s->C, s->stream));
+    } else {
+        CKL(launch_permute4(q_dev, reinterpret_cast<double *>(s->A.qs), s->d_perm, s->C, 1, s->stream));
+    }
     int r = solver_run_residual_on_qs(s, limit, dt_update, new_dt, rmax);
     if (r) return r;
-    CKL(launch_permute4(s->A.R, R_dev, s->d_perm, s->C, 0, s->stream));
+    if (split) {
+        CKL(launch_to_double4(reinterpret_cast<const float *>(s->A.R), s->d_tmp, s->C, s->stream));
+        CKL(launch_permute4(s->d_tmp, R_dev, s->d_perm, s->C, 0, s->stream));
+    } else {
+        CKL(launch_permute4(reinterpret_cast<const double *>(s->A.R), R_dev, s->d_perm, s->C, 0, s->stream));
+    }
     CK(cudaStreamSynchronize(s->stream));
     return EBB_OK;
 }
@@ -818,39 +880,25 @@ int ebb_profile_kernels(ebb_solver *s, int32_t n_rep, double *ms)
     h.err_key = EBB_NOERR;
     h.rec_enabled = 0;
     if ((r = solver_write_state(s, h))) return r;
-    // work on a copy of the state so the resident solution is untouched
-    CK(cudaMemcpyAsync(s->A.qs, s->A.q, sizeof(double) * 4 * (s->C + s->G), cudaMemcpyDeviceToDevice, s->stream));
-    cudaEvent_t ev[2];
-    CK(cudaEventCreate(&ev[0]));
-    CK(cudaEventCreate(&ev[1]));
-    for (int k = 0; k < 4; k++) {
-        float t = 0;
-        CK(cudaEventRecord(ev[0], s->stream));
-        for (int i = 0; i < n_rep; i++) {
-            if (k == 0) CKL(launch_cell_fp64(s->M, s->P, s->A, s->A.qs, s->A.qs, 1, s->stream));
-            if (k == 1) CKL(launch_flux_fp64(s->M, s->P, s->A, s->A.qs, s->stream));
-            if (k == 2) CKL(launch_update_fp64(s->M, s->P, s->A, ST_RK2_1, s->A.qs, s->A.face, 1, 1, 0, s->stream));
-            if (k == 3) CKL(launch_step_end(s->M, s->A, s->nred, s->stream));
-        }
-        CK(cudaEventRecord(ev[1], s->stream));
-        CK(cudaEventSynchronize(ev[1]));
-        CK(cudaEventElapsedTime(&t, ev[0], ev[1]));
-        ms[k] = (double)t / n_rep;
-        if (k == 2) {  // the update wrote into the face array; rebuild it
-            CKL(launch_cell_fp64(s->M, s->P, s->A, s->A.qs, s->A.qs, 1, s->stream));
-        }
-    }
-    cudaEventDestroy(ev[0]);
-    cudaEventDestroy(ev[1]);
-    return solver_write_state(s, h0);
+    r = s->precision == EBB_PREC_SPLIT ? profile_t<float>(s, n_rep, ms) : profile_t<double>(s, n_rep, ms);
+    int r2 = solver_write_state(s, h0);
+    return r ? r : r2;
 }
 
 int ebb_get_face_states(ebb_solver *s, double *out)
 {
     if (!s || !out) return EBB_ERR_ARG;
-    std::vector<double> f(4 * (size_t)s->maxJ * s->Cs);
-    CK(cudaMemcpyAsync(f.data(), s->A.face, f.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
-    CK(cudaStreamSynchronize(s->stream));
+    const size_t n = 4 * (size_t)s->maxJ * s->Cs;
+    std::vector<double> f(n);
+    if (s->precision == EBB_PREC_SPLIT) {
+        std::vector<float> g(n);
+        CK(cudaMemcpyAsync(g.data(), s->A.face, n * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        for (size_t k = 0; k < n; k++) f[k] = g[k];
+    } else {
+        CK(cudaMemcpyAsync(f.data(), s->A.face, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
     for (size_t k = 0; k < s->ref_face_slot.size(); k++)
         for (int c = 0; c < 4; c++) out[4 * k + c] = f[4 * s->ref_face_slot[k] + c];
     return EBB_OK;
@@ -893,10 +941,7 @@ int solver_run_residual_on_qs(ebb_solver *s, int limit, int dt_update, double *n
     h.done = 0;
     h.err_key = EBB_NOERR;
     if ((r = solver_write_state(s, h))) return r;
-    double *qs = s->A.qs;
-    CKL(launch_cell_fp64(s->M, s->P, s->A, qs, qs, limit, s->stream));
-    CKL(launch_flux_fp64(s->M, s->P, s->A, qs, s->stream));
-    CKL(launch_update_fp64(s->M, s->P, s->A, ST_RESID, qs, nullptr, dt_update, 1, 0, s->stream));
+    if ((r = residual_kernels(s, limit, dt_update))) return r;
     if ((r = solver_sync_state(s, h))) return r;
     if (new_dt) *new_dt = bitsd(h.newdt_bits);
     if (rmax) *rmax = bitsd(h.rmax_bits);

@@ -26,6 +26,7 @@ struct ebb_solver {
     DArrays A{};
     int32_t *d_perm = nullptr;
     double *d_stage = nullptr;  // C x 4 doubles in reference order
+    double *d_tmp = nullptr;    // C x 4 doubles in device order (split-path conversions)
     int nred = 0;
     cudaGraphExec_t g1 = nullptr, g16 = nullptr;  // 1-step and 16-step time-loop graphs
     int32_t err_kind = 0;
