@@ -609,6 +609,24 @@ __device__ __forceinline__ double warp_max(double v)
     for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
     return v;
 }
+__device__ __forceinline__ float warp_sumf(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = v + __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_minf(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_down_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ float warp_maxf(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
+    return v;
+}
 
 // Residual of one interior cell and the stage combination.  The state update runs in
 // FP64 for both precision forms.  FP64 path: qin/qout are double stage states as in
@@ -626,6 +644,8 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(DMesh M, DPhys P, DArray
     const bool act = i < M.C;
     double dtc = INFINITY, rm = 0.0;
     double ss[4] = {0, 0, 0, 0}, vs[4] = {0, 0, 0, 0};
+    float fss[4] = {0, 0, 0, 0}, fvs[4] = {0, 0, 0, 0};  // split path: FP32 lane values
+    float fdtc = INFINITY, frm = 0.0f;
     bool bad = false;
     if (act) {
         const int Cs = M.Cs;
@@ -652,12 +672,23 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(DMesh M, DPhys P, DArray
         if (need_dt || (P.local_ts && dt_update)) {
             sAve /= ld1<T>(M.g.perim, i);
             T c = ((T)st->cfl * ld1<T>(M.g.dlen, i)) / sAve;
-            if (need_dt) dtc = (double)c;
+            if (need_dt) {
+                if (SPLIT)
+                    fdtc = (float)c;
+                else
+                    dtc = (double)c;
+            }
             if (P.local_ts && dt_update) cdt[i] = isnan(c) ? T(0.0) : c;
         }
+        if (SPLIT) {
 #pragma unroll
-        for (int k = 0; k < 4; k++)
-            if ((double)fabs(r[k]) > rm) rm = (double)fabs(r[k]);
+            for (int k = 0; k < 4; k++)
+                if ((float)fabs(r[k]) > frm) frm = (float)fabs(r[k]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                if ((double)fabs(r[k]) > rm) rm = (double)fabs(r[k]);
+        }
         const T s = ld1<T>(M.g.neg_inv_area, i);
         T R[4];
 #pragma unroll
@@ -670,6 +701,69 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(DMesh M, DPhys P, DArray
         }
         if (ST == ST_RESID) {
             st4(reinterpret_cast<T *>(A.R) + 4 * (size_t)i, R);
+        } else if constexpr (SPLIT) {
+            // increments at the precision of R; the state accumulation u += inc in FP64
+            T *aux = reinterpret_cast<T *>(A.aux);
+            double q0[4];
+            ld4(A.q64 + 4 * (size_t)i, q0);
+            const float dtf = (float)st->dt, hf = P.local_ts ? (float)cdt[i] : dtf;
+            float inc[4];
+            if (ST == ST_EULER || ST == ST_TVD_1) {
+                if (ST == ST_TVD_1) st4(aux + 4 * (size_t)i, R);
+#pragma unroll
+                for (int k = 0; k < 4; k++) inc[k] = hf * R[k];
+            } else if (ST == ST_RK2_1) {
+                st4(aux + 4 * (size_t)i, R);
+#pragma unroll
+                for (int k = 0; k < 4; k++) inc[k] = dtf * R[k];
+            } else if (ST == ST_RK2_2) {
+                T k1[4];
+                ld4(aux + 4 * (size_t)i, k1);
+                const float hh = P.local_ts ? hf * 0.5f : (float)st->dt_half;
+#pragma unroll
+                for (int k = 0; k < 4; k++) inc[k] = hh * (k1[k] + R[k]);
+            } else if (ST == ST_TVD_2) {  // 0.5 (q + (q + h R1) + h R2) = q + 0.5 h (R1 + R2)
+                T r1[4];
+                ld4(aux + 4 * (size_t)i, r1);
+#pragma unroll
+                for (int k = 0; k < 4; k++) inc[k] = (0.5f * hf) * (r1[k] + R[k]);
+            } else if (ST == ST_RK4_1) {
+                st4(aux + 4 * (size_t)i, R);
+#pragma unroll
+                for (int k = 0; k < 4; k++) inc[k] = (float)st->dt_half * R[k];
+            } else if (ST == ST_RK4_2 || ST == ST_RK4_3) {
+                T acc[4];
+                ld4(aux + 4 * (size_t)i, acc);
+#pragma unroll
+                for (int k = 0; k < 4; k++) acc[k] = acc[k] + 2.0f * R[k];
+                st4(aux + 4 * (size_t)i, acc);
+                const float h2 = ST == ST_RK4_2 ? (float)st->dt_half : dtf;
+#pragma unroll
+                for (int k = 0; k < 4; k++) inc[k] = h2 * R[k];
+            } else {  // ST_RK4_4
+                T acc[4];
+                ld4(aux + 4 * (size_t)i, acc);
+                const float hh = P.local_ts ? hf / 6.0f : (float)st->dt_sixth;
+#pragma unroll
+                for (int k = 0; k < 4; k++) inc[k] = hh * (acc[k] + R[k]);
+            }
+            double out[4];
+            T o[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                out[k] = q0[k] + (double)inc[k];
+                o[k] = (T)out[k];
+            }
+            st4(qout + 4 * (size_t)i, o);
+            if (final_stage) {
+                st4(A.q64 + 4 * (size_t)i, out);
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    fss[k] = inc[k] * inc[k];
+                    fvs[k] = o[k];
+                }
+                bad = isnan(out[0]) || isnan(out[1]) || isnan(out[2]) || isnan(out[3]);
+            }
         } else {
             T *aux = reinterpret_cast<T *>(A.aux);
             double q0[4], Rd[4], out[4];
@@ -763,13 +857,25 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(DMesh M, DPhys P, DArray
     if (bad) flag_error(st, 3, ERR_NAN_CELL, (unsigned)M.cell_ref[i]);
     // block reductions: dt (min), Rmax (max), RMS partials (sum) in a fixed tree
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    dtc = warp_min(dtc);
-    rm = warp_max(rm);
-    if (final_stage) {
+    if (SPLIT) {  // 32-lane partials in FP32, block and grid accumulation in FP64
+        dtc = (double)warp_minf(fdtc);
+        rm = (double)warp_maxf(frm);
+        if (final_stage) {
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
-            ss[k] = warp_sum(ss[k]);
-            vs[k] = warp_sum(vs[k]);
+            for (int k = 0; k < 4; k++) {
+                ss[k] = (double)warp_sumf(fss[k]);
+                vs[k] = (double)warp_sumf(fvs[k]);
+            }
+        }
+    } else {
+        dtc = warp_min(dtc);
+        rm = warp_max(rm);
+        if (final_stage) {
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                ss[k] = warp_sum(ss[k]);
+                vs[k] = warp_sum(vs[k]);
+            }
         }
     }
     if (lane == 0) {
