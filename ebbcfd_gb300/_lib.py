@@ -9,6 +9,7 @@ import os
 from . import build as _build
 
 MAX_BC = 32
+FLUX_NOALLOC_MAX = 32768
 MAX_FORCE = 8
 TAG_LEN = 64
 PATH_LEN = 1024
@@ -105,6 +106,7 @@ SIGNATURES = {
     "ebb_get_stream": (C.c_int, [_vp, C.POINTER(_vp)]),
     "ebb_profile_kernels": (C.c_int, [_vp, C.c_int32, _dp]),
     "ebb_flux": (C.c_int, [C.c_int32, C.c_int64, _dp, _dp, _dp, _dp, _dp]),
+    "ebb_flux_noalloc": (C.c_int, [C.c_int32, C.c_int64, _dp, _dp, _dp, _dp, _dp]),
     "ebb_save_solution": (C.c_int, [_vp, _cp]),
     "ebb_load_solution": (C.c_int, [_vp, _cp]),
 }

@@ -20,6 +20,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU = {
     "k_fp64.cu": ["-fmad=false"],
     "k_split.cu": ["-fmad=true"],
+    "flux_noalloc.cu": ["-fmad=false"],
 }
 CPP = ["solver.cpp", "host_mesh.cpp", "host_config.cpp", "host_io.cpp"]
 

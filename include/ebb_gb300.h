@@ -34,6 +34,7 @@ extern "C" {
 #define EBB_MAX_FORCE_TAGS 8
 #define EBB_TAG_LEN 64
 #define EBB_PATH_LEN 1024
+#define EBB_FLUX_NOALLOC_MAX 32768
 
 typedef enum {
     EBB_OK = 0,
@@ -224,6 +225,19 @@ int ebb_profile_kernels(ebb_solver *s, int32_t n_rep, double *ms);
    qL,qR[n][4], normal[n][2] -> F[n][4], s_max[n]. */
 int ebb_flux(int32_t kind, int64_t n, const double *qL, const double *qR, const double *normal, double *F,
              double *s_max);
+/* Same evaluation and results as ebb_flux, for callers that cannot allocate device
+   memory when they call: ebb_flux allocates (and frees) device staging buffers on
+   every call, which is not allowed for example while another thread is capturing a
+   CUDA graph on the device in the global capture mode, and fails when a serving
+   process has reserved all device memory for its solver arenas.  This variant has no
+   counterpart in the reference.  It stages through one fixed array compiled into the
+   library (EBB_FLUX_NOALLOC_MAX faces, 3.75 MiB held on every GPU that loads the
+   library until the process exits) and returns EBB_ERR_LIMIT for n larger than
+   EBB_FLUX_NOALLOC_MAX.  Its first call on a device looks up the array's device
+   address for that device; make that first call before any stream capture.  Calls
+   share the array: calls that overlap on the same GPU race and must be serialised. */
+int ebb_flux_noalloc(int32_t kind, int64_t n, const double *qL, const double *qR, const double *normal, double *F,
+                     double *s_max);
 
 /* ---- files ---------------------------------------------------------------- */
 int ebb_save_solution(ebb_solver *s, const char *path);
