@@ -107,7 +107,7 @@ SIGNATURES = {
     "ebb_profile_kernels": (C.c_int, [_vp, C.c_int32, _dp]),
     "ebb_flux": (C.c_int, [C.c_int32, C.c_int64, _dp, _dp, _dp, _dp, _dp]),
     "ebb_flux_noalloc": (C.c_int, [C.c_int32, C.c_int64, _dp, _dp, _dp, _dp, _dp]),
-    "ebb_save_solution": (C.c_int, [_vp, _cp]),
+    "ebb_save_solution": (C.c_int, [_vp, _cp, C.c_double, C.c_double]),
     "ebb_load_solution": (C.c_int, [_vp, _cp]),
 }
 

@@ -15,11 +15,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libebbgb300.so")
+CLI = os.path.join(OUT, "ebb-solve")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU = {
     "k_fp64.cu": ["-fmad=false"],
-    "k_split.cu": ["-fmad=true"],
+    "k_split.cu": ["-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"],
     "flux_noalloc.cu": ["-fmad=false"],
 }
 CPP = ["solver.cpp", "host_mesh.cpp", "host_config.cpp", "host_io.cpp"]
@@ -37,17 +38,17 @@ def _cuda_home(nvcc):
 
 
 def _sources():
-    srcs = [os.path.join(CSRC, f) for f in list(CU) + CPP]
+    srcs = [os.path.join(CSRC, f) for f in list(CU) + CPP + ["ebb_solve.cpp"]]
     hdr = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".hpp", ".cuh"))]
     hdr.append(os.path.join(os.path.dirname(HERE), "include", "ebb_gb300.h"))
     return srcs, hdr
 
 
 def up_to_date():
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(CLI):
         return False
     srcs, hdr = _sources()
-    t = os.path.getmtime(LIB)
+    t = min(os.path.getmtime(LIB), os.path.getmtime(CLI))
     return all(os.path.getmtime(f) <= t for f in srcs + hdr + [os.path.abspath(__file__)])
 
 
@@ -87,6 +88,14 @@ def build(force=False, verbose=False):
     if p.returncode != 0:
         raise RuntimeError("link failed: %s\n%s" % (" ".join(cmd), p.stdout))
     os.replace(tmp, LIB)
+    # the ebb-solve command-line driver, linked against the library (rpath $ORIGIN)
+    tmp = CLI + ".tmp%d" % os.getpid()
+    cmd = ["g++", "-O2", "-std=c++17", "-o", tmp, os.path.join(CSRC, "ebb_solve.cpp"), "-L" + OUT, "-lebbgb300",
+           "-Wl,-rpath,$ORIGIN"]
+    p = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if p.returncode != 0:
+        raise RuntimeError("ebb-solve link failed: %s\n%s" % (" ".join(cmd), p.stdout))
+    os.replace(tmp, CLI)
     if verbose:
         print("built", LIB)
     return LIB

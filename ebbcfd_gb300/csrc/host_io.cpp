@@ -91,7 +91,7 @@ struct RD {
 
 extern "C" {
 
-int ebb_save_solution(ebb_solver *s, const char *path)
+int ebb_save_solution(ebb_solver *s, const char *path, double t, double dt)
 {
     if (!s || !path) return EBB_ERR_ARG;
     const int64_t C = s->C;
@@ -99,9 +99,6 @@ int ebb_save_solution(ebb_solver *s, const char *path)
     int r = ebb_get_state(s, q.data());
     if (r) return r;
     if ((r = ebb_get_face_states(s, f.data()))) return r;
-    double t, dt;
-    int64_t it;
-    if ((r = ebb_get_time(s, &t, &dt, &it))) return r;
     BE w;
     w.b.reserve(40 + C * (5 + 32) + f.size() * 8);
     w.u32(0xEA98E1F5u);

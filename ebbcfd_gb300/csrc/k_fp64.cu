@@ -78,6 +78,9 @@ template <typename T> __global__ void __launch_bounds__(EBB_RED_THREADS) k_step_
     st->done = !(st->t < st->t_end);
     st->dt_half = st->dt / 2.0;
     st->dt_sixth = st->dt / 6.0;
+    st->dtf = (float)st->dt;
+    st->dt_half_f = (float)st->dt_half;
+    st->dt_sixth_f = (float)st->dt_sixth;
     st->newdt_bits = 0x7FF0000000000000ull;  // +inf
     st->rmax_bits = 0ull;
 }

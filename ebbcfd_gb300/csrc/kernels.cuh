@@ -300,6 +300,38 @@ __global__ void __launch_bounds__(128) k_cell(DMesh M, DPhys P, DArrays A, const
         g[k][1] = T(0.0);
     }
     const bool second = P.order > 1;
+    if constexpr (sizeof(T) == 4) {
+        // all index and neighbour-state loads in flight before any dependent math
+        int nbv[MJ];
+        T qv[MJ][4];
+        typename V2<T>::t gmv[MJ];
+#pragma unroll
+        for (int j = 0; j < MJ; j++) nbv[j] = (j < ne) ? M.s_nbr[(size_t)j * Cs + i] : i;
+#pragma unroll
+        for (int j = 0; j < MJ; j++) {
+            ld4(qin + 4 * (size_t)(nbv[j] < M.C ? nbv[j] : i), qv[j]);
+            gmv[j] = ld2<T>(M.g.s_gm, (size_t)j * Cs + i);
+        }
+#pragma unroll
+        for (int j = 0; j < MJ; j++) {
+            if (j < ne) {
+                if (nbv[j] >= M.C) {
+                    ghost_state<T>(M, P, A.st, nbv[j] - M.C, qi, qv[j]);
+                    st4(qghost + 4 * (size_t)nbv[j], qv[j]);
+                }
+                if (second) {
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        mn[k] = fmin(mn[k], qv[j][k]);
+                        mx[k] = fmax(mx[k], qv[j][k]);
+                        T du = qv[j][k] - qi[k];
+                        g[k][0] = g[k][0] + gmv[j].x * du;
+                        g[k][1] = g[k][1] + gmv[j].y * du;
+                    }
+                }
+            }
+        }
+    } else {
 #pragma unroll
     for (int j = 0; j < MJ; j++) {
         if (j < ne) {
@@ -324,6 +356,7 @@ __global__ void __launch_bounds__(128) k_cell(DMesh M, DPhys P, DArrays A, const
                 }
             }
         }
+    }
     }
     T lim0[4] = {T(1.0), T(1.0), T(1.0), T(1.0)}, lim1[4] = {T(1.0), T(1.0), T(1.0), T(1.0)};
     if (second && P.limited && limit) {
@@ -702,11 +735,11 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(DMesh M, DPhys P, DArray
         if (ST == ST_RESID) {
             st4(reinterpret_cast<T *>(A.R) + 4 * (size_t)i, R);
         } else if constexpr (SPLIT) {
-            // increments at the precision of R; the state accumulation u += inc in FP64
+            // increments at the precision of R.  Intermediate stage inputs are FP32
+            // (the FP32 shadow of the solution plus the increment); the final stage
+            // accumulates the solution u += inc in FP64 and refreshes the shadow.
             T *aux = reinterpret_cast<T *>(A.aux);
-            double q0[4];
-            ld4(A.q64 + 4 * (size_t)i, q0);
-            const float dtf = (float)st->dt, hf = P.local_ts ? (float)cdt[i] : dtf;
+            const float dtf = st->dtf, hf = P.local_ts ? (float)cdt[i] : dtf;
             float inc[4];
             if (ST == ST_EULER || ST == ST_TVD_1) {
                 if (ST == ST_TVD_1) st4(aux + 4 * (size_t)i, R);
@@ -719,7 +752,7 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(DMesh M, DPhys P, DArray
             } else if (ST == ST_RK2_2) {
                 T k1[4];
                 ld4(aux + 4 * (size_t)i, k1);
-                const float hh = P.local_ts ? hf * 0.5f : (float)st->dt_half;
+                const float hh = P.local_ts ? hf * 0.5f : st->dt_half_f;
 #pragma unroll
                 for (int k = 0; k < 4; k++) inc[k] = hh * (k1[k] + R[k]);
             } else if (ST == ST_TVD_2) {  // 0.5 (q + (q + h R1) + h R2) = q + 0.5 h (R1 + R2)
@@ -730,40 +763,46 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(DMesh M, DPhys P, DArray
             } else if (ST == ST_RK4_1) {
                 st4(aux + 4 * (size_t)i, R);
 #pragma unroll
-                for (int k = 0; k < 4; k++) inc[k] = (float)st->dt_half * R[k];
+                for (int k = 0; k < 4; k++) inc[k] = st->dt_half_f * R[k];
             } else if (ST == ST_RK4_2 || ST == ST_RK4_3) {
                 T acc[4];
                 ld4(aux + 4 * (size_t)i, acc);
 #pragma unroll
                 for (int k = 0; k < 4; k++) acc[k] = acc[k] + 2.0f * R[k];
                 st4(aux + 4 * (size_t)i, acc);
-                const float h2 = ST == ST_RK4_2 ? (float)st->dt_half : dtf;
+                const float h2 = ST == ST_RK4_2 ? st->dt_half_f : dtf;
 #pragma unroll
                 for (int k = 0; k < 4; k++) inc[k] = h2 * R[k];
             } else {  // ST_RK4_4
                 T acc[4];
                 ld4(aux + 4 * (size_t)i, acc);
-                const float hh = P.local_ts ? hf / 6.0f : (float)st->dt_sixth;
+                const float hh = P.local_ts ? hf / 6.0f : st->dt_sixth_f;
 #pragma unroll
                 for (int k = 0; k < 4; k++) inc[k] = hh * (acc[k] + R[k]);
             }
-            double out[4];
             T o[4];
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                out[k] = q0[k] + (double)inc[k];
-                o[k] = (T)out[k];
-            }
-            st4(qout + 4 * (size_t)i, o);
             if (final_stage) {
+                double q0[4], out[4];
+                ld4(A.q64 + 4 * (size_t)i, q0);
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    out[k] = q0[k] + (double)inc[k];
+                    o[k] = (T)out[k];
+                }
                 st4(A.q64 + 4 * (size_t)i, out);
 #pragma unroll
                 for (int k = 0; k < 4; k++) {
                     fss[k] = inc[k] * inc[k];
                     fvs[k] = o[k];
                 }
-                bad = isnan(out[0]) || isnan(out[1]) || isnan(out[2]) || isnan(out[3]);
+                bad = isnan(o[0]) || isnan(o[1]) || isnan(o[2]) || isnan(o[3]);
+            } else {
+                T q32[4];
+                ld4(reinterpret_cast<const T *>(A.qs1) + 4 * (size_t)i, q32);
+#pragma unroll
+                for (int k = 0; k < 4; k++) o[k] = q32[k] + inc[k];
             }
+            st4(qout + 4 * (size_t)i, o);
         } else {
             T *aux = reinterpret_cast<T *>(A.aux);
             double q0[4], Rd[4], out[4];
@@ -858,15 +897,49 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(DMesh M, DPhys P, DArray
     // block reductions: dt (min), Rmax (max), RMS partials (sum) in a fixed tree
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (SPLIT) {  // 32-lane partials in FP32, block and grid accumulation in FP64
-        dtc = (double)warp_minf(fdtc);
-        rm = (double)warp_maxf(frm);
+        fdtc = warp_minf(fdtc);
+        frm = warp_maxf(frm);
         if (final_stage) {
 #pragma unroll
             for (int k = 0; k < 4; k++) {
-                ss[k] = (double)warp_sumf(fss[k]);
-                vs[k] = (double)warp_sumf(fvs[k]);
+                fss[k] = warp_sumf(fss[k]);
+                fvs[k] = warp_sumf(fvs[k]);
             }
         }
+        // whole block in FP32 (an FP64 instruction costs a warp the same with one lane
+        // active as with 32), one conversion per block; the grid-wide accumulation of
+        // the block partials is FP64
+        __shared__ float shf[UPD_THREADS / 32][10];
+        if (lane == 0) {
+            shf[w][0] = fdtc;
+            shf[w][1] = frm;
+            for (int k = 0; k < 4; k++) {
+                shf[w][2 + k] = fss[k];
+                shf[w][6 + k] = fvs[k];
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float a = shf[0][0], b = shf[0][1];
+            float s8[8];
+            for (int k = 0; k < 8; k++) s8[k] = shf[0][2 + k];
+            for (int ww = 1; ww < UPD_THREADS / 32; ww++) {
+                a = fminf(a, shf[ww][0]);
+                b = fmaxf(b, shf[ww][1]);
+                for (int k = 0; k < 8; k++) s8[k] = s8[k] + shf[ww][2 + k];
+            }
+            if (need_dt && a == a) {
+                const double ad = (double)a;
+                atomicMin(&st->newdt_bits, (unsigned long long)__double_as_longlong(ad));
+            }
+            if (b > 0) {
+                const double bd = (double)b;
+                atomicMax(&st->rmax_bits, (unsigned long long)__double_as_longlong(bd));
+            }
+            if (final_stage)
+                for (int k = 0; k < 8; k++) A.red[8 * (size_t)blockIdx.x + k] = (double)s8[k];
+        }
+        return;
     } else {
         dtc = warp_min(dtc);
         rm = warp_max(rm);

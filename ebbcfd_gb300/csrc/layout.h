@@ -64,7 +64,7 @@ struct DState {
     double rot[4];
     int64_t n_rec;
     int32_t rec_enabled;
-    int32_t pad;
+    float dtf, dt_half_f, dt_sixth_f;  // FP32 copies for the split path's increments
 };
 
 // record layout matches ebb_step_record

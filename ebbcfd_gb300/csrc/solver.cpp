@@ -640,6 +640,9 @@ int ebb_solver_create(const ebb_mesh *mesh, const ebb_config *cfg, int32_t preci
     h.t_end = cfg->t_end;
     h.dt_half = h.dt / 2.0;
     h.dt_sixth = h.dt / 6.0;
+    h.dtf = (float)h.dt;
+    h.dt_half_f = (float)h.dt_half;
+    h.dt_sixth_f = (float)h.dt_sixth;
     h.newdt_bits = 0x7FF0000000000000ull;
     h.rmax_bits = 0;
     h.err_key = EBB_NOERR;
@@ -729,6 +732,9 @@ int ebb_set_time(ebb_solver *s, double t, double dt)
     h.dt = dt;
     h.dt_half = dt / 2.0;
     h.dt_sixth = dt / 6.0;
+    h.dtf = (float)dt;
+    h.dt_half_f = (float)h.dt_half;
+    h.dt_sixth_f = (float)h.dt_sixth;
     h.done = !(h.t < h.t_end);
     return solver_write_state(s, h);
 }
@@ -778,6 +784,9 @@ int ebb_step(ebb_solver *s, double *dt, double *rmax)
     h.dt = *dt;
     h.dt_half = *dt / 2.0;
     h.dt_sixth = *dt / 6.0;
+    h.dtf = (float)*dt;
+    h.dt_half_f = (float)h.dt_half;
+    h.dt_sixth_f = (float)h.dt_sixth;
     h.newdt_bits = 0x7FF0000000000000ull;
     h.rmax_bits = (*rmax > 0) ? dbits(*rmax) : 0ull;
     h.done = 0;

@@ -257,8 +257,13 @@ class UfvmSolver:
         self._raise(_lib.load().ebb_get_face_states(self.h, _dp(out)))
         return out
 
-    def save_solution(self, path):
-        self._raise(_lib.load().ebb_save_solution(self.h, str(path).encode()))
+    def save_solution(self, path, t=None, dt=None):
+        """io.d:68 saveSolution; t and dt default to the solver's current time and step."""
+        if t is None or dt is None:
+            t0, dt0, _ = self.time()
+            t = t0 if t is None else t
+            dt = dt0 if dt is None else dt
+        self._raise(_lib.load().ebb_save_solution(self.h, str(path).encode(), float(t), float(dt)))
 
     def load_solution(self, path):
         self._raise(_lib.load().ebb_load_solution(self.h, str(path).encode()))

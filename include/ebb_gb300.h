@@ -240,7 +240,9 @@ int ebb_flux_noalloc(int32_t kind, int64_t n, const double *qL, const double *qR
                      double *s_max);
 
 /* ---- files ---------------------------------------------------------------- */
-int ebb_save_solution(ebb_solver *s, const char *path);
+/* .esln v2 of the resident state with the header time t and step dt (saveSolution
+   takes them as arguments: the driver saves before advancing t). */
+int ebb_save_solution(ebb_solver *s, const char *path, double t, double dt);
 int ebb_load_solution(ebb_solver *s, const char *path);
 
 #ifdef __cplusplus
