@@ -49,10 +49,10 @@ def read_frc(path):
 def plate_dir(tmp_path):
     shutil.copy(os.path.join(MESHES, "flatPlate_0.msh"), tmp_path / "flatPlate_0.msh")
     d = json.load(open(os.path.join(MESHES, "flatPlate_0.json")))
-    d["plotIter"] = 10
-    d["saveIter"] = 25
+    d["plotIter"] = 3
+    d["saveIter"] = 4
     d["dt"] = 1e-5
-    d["tEnd"] = 0.06
+    d["tEnd"] = 0.25
     (tmp_path / "cfg.json").write_text(json.dumps(d))
     return tmp_path, d
 
@@ -65,7 +65,7 @@ def test_ebb_solve_run_and_restart(plate_dir):
     assert "Running 2D finite volume solver" in p.stdout and "-flux: roeFlux" in p.stdout
     frc = read_frc(tmp / "boundaryForces.frc")
     n = len(frc)
-    assert n > 30
+    assert n >= 9
     # the oracle runs the same loop
     conf = gmsh_ref.load_config(json.dumps(d))
     om = ref.OracleMesh(gmsh_ref.parse_gmsh(str(tmp / "flatPlate_0.msh")), conf)
@@ -85,9 +85,9 @@ def test_ebb_solve_run_and_restart(plate_dir):
     assert (np.abs(fin["faces"] - of).max(axis=0) / np.abs(of).max(axis=0)).max() <= 1e-9
     # save files every saveIter iterations, including iteration 0
     saves = sorted(f for f in os.listdir(tmp) if f.startswith("save_"))
-    assert saves == ["save_%d_0.esln" % k for k in range((n - 1) // 25 + 1)]
+    assert saves == ["save_%d_0.esln" % k for k in range((n - 1) // 4 + 1)]
     s1 = read_esln(tmp / "save_1_0.esln")
-    assert s1["t"] == rec[25, 0] and s1["dt"] == rec[25, 8]
+    assert s1["t"] == rec[4, 0] and s1["dt"] == rec[4, 8]
     # restart from save_1_ continues at that t
     p2 = subprocess.run([B.CLI, "-c", "cfg.json", "-s", "save_1_"], cwd=tmp, capture_output=True, text=True,
                         timeout=300)
