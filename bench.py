@@ -247,6 +247,93 @@ def cpu_baseline(gen, ncell, budget_s=20.0, steps_max=1000):
             "sample": "%d RK2 steps of the full %d-cell wedge (after 1 untimed step)" % (n, ncell)}
 
 
+def mms32_config():
+    return json.dumps({"mesh": "quads32.msh", "dt": 1e-4, "tEnd": 1e9, "flux": "roeFlux", "saveIter": -1,
+                       "plotIter": -1, "forceBoundary": "Freestream", "integrator": "RK2_TVD", "limited": True,
+                       "CFL": 0.5, "cflAdjust": False, "initialConditions": [0.5, 0, 1, 1],
+                       "boudaryConditions": [{"tag": "Freestream", "type": "dirichlet", "q": [0.5, 0, 1, 1]}]})
+
+
+def plate_config():
+    bcs = [{"tag": "Inflow", "type": "fullState", "q": [0.3, 0, 1, 1]},
+           {"tag": "Top", "type": "fullState", "q": [0.3, 0, 1, 1]},
+           {"tag": "Outflow", "type": "constP", "q": [1.0 / (1.4 * 0.09)]},
+           {"tag": "Symmetry", "type": "symmetry", "q": [0.3, 0, 1, 1]},
+           {"tag": "Wall", "type": "viscidWall", "q": [0.3, 0, 1, 1]}]
+    return json.dumps({"mesh": "plate.msh", "dt": 1e-7, "tEnd": 1e9, "flux": "roeFlux", "saveIter": -1,
+                       "plotIter": -1, "forceBoundary": "Wall", "integrator": "RK4", "limited": True, "CFL": 0.8,
+                       "cflAdjust": False, "viscosity": True,
+                       "physicalConfig": {"Pr": 0.72, "R": 1.0, "gamma": 1.4, "Re": 1e5, "L": 1.0},
+                       "initialConditions": [0.3, 0, 1, 1], "boudaryConditions": bcs})
+
+
+def run_mms32(args):
+    """32x32 quads on [0,1]^2, the sine manufactured fields, Dirichlet boundaries, Roe,
+    limited, TVD-RK2, CFL 0.5, 1000 steps: L2(rho) error vs the exact field for the
+    oracle, the plain FP64 path (which must equal it bitwise) and the split path."""
+    import ctypes as C
+    import ebbcfd_gb300 as E
+    from ebbcfd_gb300 import _lib, meshgen
+    from oracle import gmsh_ref, ref
+    L = _lib.load()
+    gen = meshgen.uniform_quads(32)
+    steps = args.steps if args.steps_given else 1000
+    out = {"workload": "mms32-sine-roe-tvd-cfl0.5", "cells": 1024, "steps": steps}
+    q_exact, _, _ = ref.mms_eval(2, gen.to_solver_mesh().centroids())
+    for prec in ("fp64", "split"):
+        cfg = E.load_config(mms32_config())
+        cfg.mms = 2
+        sol = E.UfvmSolver(gen.to_solver_mesh(), cfg, precision=prec)
+        n = C.c_int64()
+        ms = C.c_double()
+        L.ebb_run_timed(sol.h, steps, C.byref(n), C.byref(ms))
+        q = sol.state
+        out[prec] = {"l2_rho": float(np.sqrt(np.mean((q[:, 0] - q_exact[:, 0]) ** 2))), "steps": n.value,
+                     "cell_updates_per_s": 1024 * n.value / (ms.value / 1e3), "state": q}
+    om = ref.OracleMesh(gen.as_reader_dict(), gmsh_ref.load_config(mms32_config()), mms=2)
+    om.run(steps)
+    qo = om.state()
+    out["oracle"] = {"l2_rho": float(np.sqrt(np.mean((qo[:, 0] - q_exact[:, 0]) ** 2)))}
+    out["fp64_equals_oracle_bitwise"] = bool(np.array_equal(out["fp64"]["state"], qo))
+    out["split_l2_rel_diff"] = abs(out["split"]["l2_rho"] / out["fp64"]["l2_rho"] - 1)
+    for prec in ("fp64", "split"):
+        del out[prec]["state"]
+    return out
+
+
+def run_plate(args):
+    """Navier-Stokes laminar flat plate on ~4.0M mixed cells: both precision forms
+    from the same start, throughput and the split path's drag error against FP64."""
+    import ctypes as C
+    import ebbcfd_gb300 as E
+    from ebbcfd_gb300 import _lib, meshgen
+    L = _lib.load()
+    t0 = time.time()
+    gen = meshgen.flat_plate(args.cells if args.cells_given else 4_000_000)
+    mesh = gen.to_solver_mesh()
+    mesh_s = time.time() - t0
+    steps = args.steps if args.steps_given else 200
+    out = {"workload": "ns-plate-M0.3-Re1e5-roe-rk4-cfl0.8", "cells": mesh.n_cells, "mesh_s": round(mesh_s, 1),
+           "steps": steps}
+    recs = {}
+    for prec in ("fp64", "split"):
+        sol = E.UfvmSolver(mesh, E.load_config(plate_config()), precision=prec)
+        sol.run(args.warmup, records=False)
+        n = C.c_int64()
+        ms = C.c_double()
+        code = L.ebb_run_timed(sol.h, steps, C.byref(n), C.byref(ms))
+        if code:
+            sol._raise(code)
+        rec = sol.run(1)
+        recs[prec] = rec[-1]
+        out[prec] = {"cell_updates_per_s": mesh.n_cells * n.value / (ms.value / 1e3), "ms_per_step": ms.value / n.value,
+                     "drag": float(rec[-1][1]), "lift": float(rec[-1][2])}
+        sol.close()
+    out["split_speedup"] = out["split"]["cell_updates_per_s"] / out["fp64"]["cell_updates_per_s"]
+    out["split_drag_rel_err"] = abs(out["split"]["drag"] / out["fp64"]["drag"] - 1)
+    return out
+
+
 def run_reference(args, ws, rank):
     from ebbcfd_gb300 import meshgen
     from oracle import gmsh_ref, ref
@@ -289,6 +376,11 @@ def main():
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     ws, rank, local = dist_env()
+    if args.workload != "wedge":
+        # accuracy/throughput reports for the other configurations (not the headline line)
+        out = run_mms32(args) if args.workload == "mms32" else run_plate(args)
+        print(json.dumps(out))
+        return
     if args.impl == "reference":
         if rank == 0:
             print(json.dumps(run_reference(args, ws, rank)))
