@@ -373,7 +373,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-split", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--workload", default="wedge", choices=["wedge", "mms32", "plate4m"])
     args = ap.parse_args()
+    args.steps_given = "--steps" in sys.argv
+    args.cells_given = "--cells" in sys.argv
     args.warmup = max(3, args.warmup)
     ws, rank, local = dist_env()
     if args.workload != "wedge":
