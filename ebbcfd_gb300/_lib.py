@@ -69,6 +69,32 @@ class StepRecord(C.Structure):
                 ("rmax", C.c_double), ("dt", C.c_double), ("cfl", C.c_double)]
 
 
+class InstanceStatus(C.Structure):
+    _fields_ = [("cell_offset", C.c_int64), ("n_cells", C.c_int64), ("iterations", C.c_int64),
+                ("t", C.c_double), ("dt", C.c_double), ("cfl", C.c_double), ("done", C.c_int32),
+                ("status", C.c_int32), ("err_index", C.c_int64), ("drag", C.c_double), ("lift", C.c_double),
+                ("resid", C.c_double * 4), ("rmax", C.c_double), ("resid_first", C.c_double)]
+
+
+class ServerOptions(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("max_arenas", C.c_int32), ("max_batch", C.c_int32),
+                ("build_threads", C.c_int32), ("tick_ms", C.c_double), ("size_ratio", C.c_double),
+                ("arena_cells", C.c_int64), ("hbm_budget", C.c_uint64)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("id", C.c_int64), ("status", C.c_int32), ("done_reason", C.c_int32), ("err_index", C.c_int64),
+                ("n_cells", C.c_int64), ("iterations", C.c_int64), ("t", C.c_double), ("drag", C.c_double),
+                ("lift", C.c_double), ("resid", C.c_double * 4), ("resid_first", C.c_double),
+                ("submit_s", C.c_double), ("admit_s", C.c_double), ("finish_s", C.c_double), ("msg", C.c_char * 96)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("bytes_in_use", C.c_uint64), ("bytes_peak", C.c_uint64), ("arenas", C.c_int32),
+                ("waiting", C.c_int32), ("building", C.c_int32), ("reserved", C.c_int32),
+                ("submitted", C.c_int64), ("finished", C.c_int64), ("cell_updates", C.c_int64)]
+
+
 # every function the header declares, with its signature
 _dp = C.POINTER(C.c_double)
 _vp = C.c_void_p
@@ -107,6 +133,25 @@ SIGNATURES = {
     "ebb_profile_kernels": (C.c_int, [_vp, C.c_int32, _dp]),
     "ebb_flux": (C.c_int, [C.c_int32, C.c_int64, _dp, _dp, _dp, _dp, _dp]),
     "ebb_flux_noalloc": (C.c_int, [C.c_int32, C.c_int64, _dp, _dp, _dp, _dp, _dp]),
+    "ebb_batch_create": (C.c_int, [C.c_int32, C.POINTER(_vp), C.POINTER(Config), C.c_int32, C.POINTER(_vp), _cp,
+                                   C.c_size_t]),
+    "ebb_batch_size": (C.c_int, [_vp, C.POINTER(C.c_int32)]),
+    "ebb_batch_status": (C.c_int, [_vp, C.c_int32, C.c_int32, C.POINTER(InstanceStatus)]),
+    "ebb_batch_set_stop": (C.c_int, [_vp, C.c_int32, C.c_double, C.c_int64, C.c_double]),
+    "ebb_batch_get_state": (C.c_int, [_vp, C.c_int32, _dp]),
+    "ebb_batch_set_state": (C.c_int, [_vp, C.c_int32, _dp]),
+    "ebb_launch_steps": (C.c_int, [_vp, C.c_int64]),
+    "ebb_sync": (C.c_int, [_vp]),
+    "ebb_batch_footprint": (C.c_int, [C.c_int32, C.POINTER(_vp), C.POINTER(Config), C.c_int32,
+                                      C.POINTER(C.c_size_t), _cp, C.c_size_t]),
+    "ebb_server_options_defaults": (None, [C.POINTER(ServerOptions)]),
+    "ebb_server_create": (C.c_int, [C.POINTER(ServerOptions), C.POINTER(_vp), _cp, C.c_size_t]),
+    "ebb_server_submit": (C.c_int, [_vp, _vp, C.POINTER(Config), C.c_int64, C.c_double, C.POINTER(C.c_int64)]),
+    "ebb_server_tick": (C.c_int, [_vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "ebb_server_results": (C.c_int, [_vp, C.POINTER(RequestResult), C.c_int32, C.POINTER(C.c_int32)]),
+    "ebb_server_take_state": (C.c_int, [_vp, C.c_int64, _dp]),
+    "ebb_server_stats_get": (C.c_int, [_vp, C.POINTER(ServerStats)]),
+    "ebb_server_destroy": (None, [_vp]),
     "ebb_save_solution": (C.c_int, [_vp, _cp, C.c_double, C.c_double]),
     "ebb_load_solution": (C.c_int, [_vp, _cp]),
 }

@@ -23,7 +23,7 @@ CU = {
     "k_split.cu": ["-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"],
     "flux_noalloc.cu": ["-fmad=false"],
 }
-CPP = ["solver.cpp", "host_mesh.cpp", "host_config.cpp", "host_io.cpp"]
+CPP = ["solver.cpp", "arena.cpp", "server.cpp", "host_mesh.cpp", "host_config.cpp", "host_io.cpp"]
 
 
 def _nvcc():

@@ -17,7 +17,12 @@ namespace {
 // a fixed tree order
 template <typename T> __global__ void __launch_bounds__(EBB_RED_THREADS) k_step_end(DMesh M, DArrays A, int nblk)
 {
-    DState *st = A.st;
+    // one block per instance
+    const int inst = blockIdx.x;
+    DState *st = A.st + inst;
+    const int b0 = M.inst_blk ? M.inst_blk[inst] : 0, b1 = M.inst_blk ? M.inst_blk[inst + 1] : nblk;
+    const int fb0 = M.force_off ? M.force_off[inst] : 0, fb1 = M.force_off ? M.force_off[inst + 1] : M.n_force;
+    const int ncell = M.inst_c0 ? M.inst_c0[inst + 1] - M.inst_c0[inst] : M.C;
     if (st->done) return;
     if (st->err_key != EBB_NOERR) {
         if (threadIdx.x == 0) st->done = 1;
@@ -26,10 +31,10 @@ template <typename T> __global__ void __launch_bounds__(EBB_RED_THREADS) k_step_
     __shared__ double sh[EBB_RED_THREADS][10];
     double s[10];
     for (int k = 0; k < 10; k++) s[k] = 0.0;
-    for (int b = threadIdx.x; b < nblk; b += EBB_RED_THREADS)
+    for (int b = b0 + threadIdx.x; b < b1; b += EBB_RED_THREADS)
         for (int k = 0; k < 8; k++) s[k] = s[k] + A.red[8 * (size_t)b + k];
     const T *fl = reinterpret_cast<const T *>(A.fl);
-    for (int f = threadIdx.x; f < M.n_force; f += EBB_RED_THREADS) {
+    for (int f = fb0 + threadIdx.x; f < fb1; f += EBB_RED_THREADS) {
         const size_t e = (size_t)M.Eint + M.force_b[f];
         s[8] = s[8] + (double)fl[4 * e + 1];
         s[9] = s[9] + (double)fl[4 * e + 2];
@@ -46,7 +51,7 @@ template <typename T> __global__ void __launch_bounds__(EBB_RED_THREADS) k_step_
     const double rmax = __longlong_as_double((long long)st->rmax_bits);
     if (st->dynamic_dt) st->dt = newdt;
     double resid[4];
-    for (int k = 0; k < 4; k++) resid[k] = sqrt((double)M.C * sh[0][k]) / sh[0][4 + k];
+    for (int k = 0; k < 4; k++) resid[k] = sqrt((double)ncell * sh[0][k]) / sh[0][4 + k];
     const double f0 = sh[0][8], f1 = sh[0][9];
     const double drag = st->rot[0] * f0 + st->rot[1] * f1;
     const double lift = st->rot[2] * f0 + st->rot[3] * f1;
@@ -62,6 +67,11 @@ template <typename T> __global__ void __launch_bounds__(EBB_RED_THREADS) k_step_
         }
     }
     st->resid_last = residMax;
+    if (st->resid_first < 0) st->resid_first = residMax;
+    st->last[0] = drag;
+    st->last[1] = lift;
+    for (int k = 0; k < 4; k++) st->last[2 + k] = resid[k];
+    st->last[6] = rmax;
     if (st->rec_enabled) {
         DRecord &r = A.rec[st->n_rec % EBB_REC_CAP];
         r.t = st->t;
@@ -75,7 +85,8 @@ template <typename T> __global__ void __launch_bounds__(EBB_RED_THREADS) k_step_
     }
     st->t += st->dt;
     st->iter++;
-    st->done = !(st->t < st->t_end);
+    st->done = !(st->t < st->t_end) || (st->max_steps > 0 && st->iter >= st->max_steps) ||
+               (st->stop_drop > 0 && residMax <= st->stop_drop * st->resid_first);
     st->dt_half = st->dt / 2.0;
     st->dt_sixth = st->dt / 6.0;
     st->dtf = (float)st->dt;
@@ -140,12 +151,15 @@ inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
 int update_blocks(int C) { return (C + UPD_THREADS - 1) / UPD_THREADS; }
 
+int update_grid(const DMesh &M) { return M.n_upd_blocks; }
+
 int launch_step_end(const DMesh &M, const DArrays &A, int nred_blocks, int split, void *stream)
 {
+    const int n = M.n_inst > 0 ? M.n_inst : 1;
     if (split)
-        k_step_end<float><<<1, EBB_RED_THREADS, 0, (cudaStream_t)stream>>>(M, A, nred_blocks);
+        k_step_end<float><<<n, EBB_RED_THREADS, 0, (cudaStream_t)stream>>>(M, A, nred_blocks);
     else
-        k_step_end<double><<<1, EBB_RED_THREADS, 0, (cudaStream_t)stream>>>(M, A, nred_blocks);
+        k_step_end<double><<<n, EBB_RED_THREADS, 0, (cudaStream_t)stream>>>(M, A, nred_blocks);
     return ret(cudaGetLastError());
 }
 

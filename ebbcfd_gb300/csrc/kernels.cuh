@@ -283,9 +283,10 @@ __device__ __forceinline__ void lp_limit(const DMesh &M, int i, int ne, const T 
 template <typename T, int MJ, bool LP>
 __global__ void __launch_bounds__(128) k_cell(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, int limit)
 {
-    if (halted(A.st)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= M.C) return;
+    DState *st = A.st + (M.cell_inst ? M.cell_inst[i] : 0);
+    if (halted(st)) return;
     const int Cs = M.Cs;
     T *qghost = const_cast<T *>(qin);  // ghost slots [C, C+G) are written by their owner only
     T qi[4];
@@ -316,7 +317,7 @@ __global__ void __launch_bounds__(128) k_cell(DMesh M, DPhys P, DArrays A, const
         for (int j = 0; j < MJ; j++) {
             if (j < ne) {
                 if (nbv[j] >= M.C) {
-                    ghost_state<T>(M, P, A.st, nbv[j] - M.C, qi, qv[j]);
+                    ghost_state<T>(M, P, st, nbv[j] - M.C, qi, qv[j]);
                     st4(qghost + 4 * (size_t)nbv[j], qv[j]);
                 }
                 if (second) {
@@ -341,7 +342,7 @@ __global__ void __launch_bounds__(128) k_cell(DMesh M, DPhys P, DArrays A, const
             if (nb < M.C) {
                 ld4(qin + 4 * (size_t)nb, qn);
             } else {
-                ghost_state<T>(M, P, A.st, nb - M.C, qi, qn);
+                ghost_state<T>(M, P, st, nb - M.C, qi, qn);
                 st4(qghost + 4 * (size_t)nb, qn);
             }
             if (second) {
@@ -459,7 +460,10 @@ __device__ void boundary_flux(const DMesh &M, const DPhys &P, const DArrays &A, 
     T F[4], sMax = 0;
     const int owner = M.b_cell[b];
     const int ghost = M.C + b;
-    const T pr = (T)P.pr, mu = (T)P.mu;
+    const int inst = M.cell_inst ? M.cell_inst[owner] : 0;
+    DState *st = A.st + inst;
+    if (halted(st)) return;
+    const T pr = (T)P.pr, mu = (T)(M.inst_mu ? M.inst_mu[inst] : P.mu);
     switch (type & 0xff) {
     case BC_DIRICHLET:
     case BC_FULLSTATE: {
@@ -577,7 +581,7 @@ __device__ void boundary_flux(const DMesh &M, const DPhys &P, const DArrays &A, 
     default:
         F[0] = F[1] = F[2] = F[3] = T(NAN);
     }
-    if (has_nan(F)) flag_error(A.st, 1, ERR_NAN_EDGE, (unsigned)M.b_ref[b]);
+    if (has_nan(F)) flag_error(st, 1, ERR_NAN_EDGE, (unsigned)M.b_ref[b]);
     const T len = ld1<T>(M.g.b_len, b);
     const size_t e = (size_t)M.Eint + b;
     T lf[4] = {len * F[0], len * F[1], len * F[2], len * F[3]};
@@ -588,7 +592,6 @@ __device__ void boundary_flux(const DMesh &M, const DPhys &P, const DArrays &A, 
 template <typename T>
 __global__ void __launch_bounds__(128) k_flux(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, int nbi)
 {
-    if (halted(A.st)) return;
     if ((int)blockIdx.x >= nbi) {
         const int b = (blockIdx.x - nbi) * blockDim.x + threadIdx.x;
         if (b < M.G) boundary_flux<T>(M, P, A, qin, b);
@@ -596,6 +599,10 @@ __global__ void __launch_bounds__(128) k_flux(DMesh M, DPhys P, DArrays A, const
     }
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= M.Eint) return;
+    int inst = 0;
+    if (M.cell_inst) inst = M.cell_inst[reinterpret_cast<const int2 *>(M.e_cell)[e].x];
+    DState *st = A.st + inst;
+    if (halted(st)) return;
     const int2 sl = reinterpret_cast<const int2 *>(M.e_slot)[e];
     const T *face = reinterpret_cast<const T *>(A.face);
     T qL[4], qR[4], F[4], sMax;
@@ -613,10 +620,10 @@ __global__ void __launch_bounds__(128) k_flux(DMesh M, DPhys P, DArrays A, const
             dq[k][0] = T(0.5) * (g1[k][0] + g2[k][0]);
             dq[k][1] = T(0.5) * (g1[k][1] + g2[k][1]);
         }
-        diffusive_flux((T)P.pr, (T)P.mu, qa, dq, n.x, n.y, Fv);
+        diffusive_flux((T)P.pr, (T)(M.inst_mu ? M.inst_mu[inst] : P.mu), qa, dq, n.x, n.y, Fv);
         for (int k = 0; k < 4; k++) F[k] = F[k] - Fv[k];
     }
-    if (has_nan(F)) flag_error(A.st, 2, ERR_NAN_EDGE, (unsigned)M.e_ref[e]);
+    if (has_nan(F)) flag_error(st, 2, ERR_NAN_EDGE, (unsigned)M.e_ref[e]);
     const T len = ld1<T>(M.g.e_len, e);
     T lf[4] = {len * F[0], len * F[1], len * F[2], len * F[3]};
     st4(reinterpret_cast<T *>(A.fl) + 4 * (size_t)e, lf);
@@ -670,11 +677,19 @@ __global__ void __launch_bounds__(UPD_THREADS) k_update(DMesh M, DPhys P, DArray
                                                        int dt_update, int need_dt, int final_stage)
 {
     constexpr bool SPLIT = sizeof(T) == 4;
-    DState *st = A.st;
+    int i, iend, inst = 0;
+    if (M.blk_first) {  // batched arena: each block lies inside one instance's cell range
+        i = M.blk_first[blockIdx.x] + threadIdx.x;
+        iend = M.blk_end[blockIdx.x];
+        inst = M.blk_inst[blockIdx.x];
+    } else {
+        i = blockIdx.x * blockDim.x + threadIdx.x;
+        iend = M.C;
+    }
+    DState *st = A.st + inst;
     if (halted(st)) return;
     __shared__ double sh[UPD_THREADS / 32][10];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool act = i < M.C;
+    const bool act = i < iend;
     double dtc = INFINITY, rm = 0.0;
     double ss[4] = {0, 0, 0, 0}, vs[4] = {0, 0, 0, 0};
     float fss[4] = {0, 0, 0, 0}, fvs[4] = {0, 0, 0, 0};  // split path: FP32 lane values
@@ -1015,7 +1030,7 @@ template <typename T>
 int launch_update_impl(const DMesh &M, const DPhys &P, const DArrays &A, int stage, const T *qin, T *qout,
                        int dt_update, int need_dt, int final_stage, void *stream)
 {
-    dim3 grid((M.C + UPD_THREADS - 1) / UPD_THREADS);
+    dim3 grid(M.n_upd_blocks);
     if (grid.x == 0) return 0;
     cudaStream_t s = (cudaStream_t)stream;
 #define EBB_UPD(S)                                                                                       \

@@ -41,6 +41,15 @@ struct DMesh {
     const int32_t *force_b;            // boundary indices summed for forces
     int32_t n_force;
     DGeo g;                            // arrays in the kernels' arithmetic type
+    // batched arena of n_inst independent instances (all null when n_inst == 1):
+    int32_t n_inst;
+    int32_t n_upd_blocks;              // k_update grid size
+    const int32_t *cell_inst;          // instance of each interior cell
+    const int32_t *blk_first, *blk_end, *blk_inst;  // k_update block -> cell range, instance
+    const int32_t *inst_c0;            // n_inst+1 interior-cell offsets
+    const int32_t *inst_blk;           // n_inst+1 k_update block offsets
+    const int32_t *force_off;          // n_inst+1 offsets into force_b
+    const double *inst_mu;             // viscosity per instance
 };
 
 struct DPhys {
@@ -65,6 +74,10 @@ struct DState {
     int64_t n_rec;
     int32_t rec_enabled;
     float dtf, dt_half_f, dt_sixth_f;  // FP32 copies for the split path's increments
+    int64_t max_steps;                 // > 0: done after this many iterations
+    double stop_drop;                  // > 0: done once residMax <= stop_drop * first residMax
+    double resid_first;                // residMax of the first iteration (< 0: not yet seen)
+    double last[7];                    // drag, lift, resid[4], Rmax of the latest iteration
 };
 
 // record layout matches ebb_step_record
@@ -116,6 +129,7 @@ template <>
 int launch_update<float>(const DMesh &, const DPhys &, const DArrays &, int, const float *, float *, int, int, int,
                          void *);
 int launch_step_end(const DMesh &M, const DArrays &A, int nred_blocks, int split, void *stream);
+int update_grid(const DMesh &M);
 int launch_flux_batch(int kind, int64_t n, const double *qL, const double *qR, const double *nrm, double *F,
                       double *s, void *stream);
 int update_blocks(int C);

@@ -15,6 +15,9 @@ tags 1..N in PhysicalNames order, triangles type 2, quads type 3.
 * ``flat_plate``: [-0.5,2]x[0,0.5]; anisotropic quads in a wall layer (first cell
   1e-4, growth 1.05) and Delaunay triangles above.  Tags: Inflow, Top, Outflow,
   Symmetry (y=0, x<0), Wall (y=0, x>=0).
+* ``cylinder``: circle of radius 0.5 at the origin in the 40 x 20 box
+  [-10,30]x[-10,10]; Delaunay triangles on rings whose spacing grows linearly with
+  the distance from the wall.  Tags: Inflow, Outflow, Top, Bottom, Cylinder.
 * ``uniform_quads``: n x n quads on [0,1]^2 with one tag (Freestream).
 """
 import math
@@ -342,6 +345,68 @@ def flat_plate(n_cells=4_000_000, h1=1e-4, growth=1.05, seed=0, layer_top=None):
     be = np.array([[r[1], r[2]] for r in allb], dtype=np.int64)
     starts = [int(np.searchsorted(g, k)) for k in range(len(tags))]
     return MeshArrays(nodes, [quads + 1, tris + 1], be, starts, tags)
+
+
+def _cylinder_points(hw, growth, box, r0, rng):
+    (x0, x1), (y0, y1) = box
+    rmax = math.hypot(max(-x0, x1), max(-y0, y1))
+    pts = []
+    r = r0
+    k = 0
+    while r < rmax:
+        h = hw * (1 + growth * (r - r0))
+        n = max(8, int(math.ceil(2 * math.pi * r / h)))
+        th = (np.arange(n) + 0.5 * (k % 2)) * (2 * math.pi / n) + rng.uniform(-0.05, 0.05) * (k > 0)
+        x, y = r * np.cos(th), r * np.sin(th)
+        m = (x > x0 + 0.5 * h) & (x < x1 - 0.5 * h) & (y > y0 + 0.5 * h) & (y < y1 - 0.5 * h)
+        pts.append(np.column_stack([x[m], y[m]]))
+        r += 0.866 * h
+        k += 1
+    return np.vstack(pts)
+
+
+def cylinder(n_cells=20000, r=0.5, seed=0, growth=0.25):
+    rng = np.random.default_rng(seed)
+    box = ((-10.0, 30.0), (-10.0, 10.0))
+
+    def count(hw):
+        return 2 * len(_cylinder_points(hw, growth, box, r, np.random.default_rng(0)))
+
+    lo, hi = 1e-4, 2.0  # wall spacing bracket
+    for _ in range(40):
+        mid = math.sqrt(lo * hi)
+        if count(mid) > n_cells:
+            lo = mid
+        else:
+            hi = mid
+    hw = math.sqrt(lo * hi)
+    ip = _cylinder_points(hw, growth, box, r, rng)
+    h_fn = lambda x, y: hw * (1 + growth * (math.hypot(x, y) - r))
+    (x0, x1), (y0, y1) = box
+    bpts = _polyline([(x0, y0), (x1, y0), (x1, y1), (x0, y1)], h_fn, closed=True)
+    nodes = np.vstack([bpts, ip])
+    tri = Delaunay(nodes).simplices.astype(np.int64)
+    c = nodes[tri].mean(axis=1)
+    tri = tri[np.hypot(c[:, 0], c[:, 1]) > r]
+    tris, a = _ccw(nodes, tri)
+    tris = tris[a > 1e-14]
+    used = np.unique(tris)
+    remap = np.full(len(nodes), -1, np.int64)
+    remap[used] = np.arange(len(used))
+    nodes, tris = nodes[used], remap[tris]
+    tags = ["Inflow", "Outflow", "Top", "Bottom", "Cylinder"]
+    eps = 1e-9
+
+    def classify(mx, my):
+        g = np.full(mx.shape, 4)
+        g[mx < x0 + eps] = 0
+        g[mx > x1 - eps] = 1
+        g[my > y1 - eps] = 2
+        g[my < y0 + eps] = 3
+        return g
+
+    be, starts = _boundary_groups(nodes, tris, classify, tags)
+    return MeshArrays(nodes, tris + 1, be, starts, tags)
 
 
 def uniform_quads(n=32):

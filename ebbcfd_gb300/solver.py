@@ -169,6 +169,8 @@ def import_mesh(path):
 class UfvmSolver:
     """Device-resident solver for one mesh + config (buildMesh + ufvmSetup)."""
 
+    n = 1  # instances in the arena
+
     def __init__(self, mesh, cfg, precision="fp64"):
         L = _lib.load()
         self.mesh = mesh
@@ -268,6 +270,22 @@ class UfvmSolver:
     def load_solution(self, path):
         self._raise(_lib.load().ebb_load_solution(self.h, str(path).encode()))
 
+    def status(self, first=0, count=None):
+        """list of dicts (cell_offset, n_cells, iterations, t, dt, cfl, done, status, err_index,
+        drag, lift, resid, rmax, resid_first) for instances first..first+count-1"""
+        count = self.n - first if count is None else count
+        arr = (_lib.InstanceStatus * max(1, count))()
+        self._raise(_lib.load().ebb_batch_status(self.h, first, count, arr))
+        out = []
+        for k in range(count):
+            d = {f: getattr(arr[k], f) for f in STATUS_FIELDS}
+            d["resid"] = list(d["resid"])
+            out.append(d)
+        return out
+
+    def set_stop(self, k=-1, t_end=1e300, max_steps=0, resid_drop=0.0):
+        self._raise(_lib.load().ebb_batch_set_stop(self.h, int(k), float(t_end), int(max_steps), float(resid_drop)))
+
 
 def _flux(kind, qL, qR, n):
     L = _lib.load()
@@ -286,3 +304,131 @@ def roe_flux(qL, qR, n):
 
 def rusanov_flux(qL, qR, n):
     return _flux(0, qL, qR, n)
+
+
+def _mesh_cfg_arrays(meshes, cfgs):
+    if isinstance(cfgs, _lib.Config):
+        cfgs = [cfgs] * len(meshes)
+    if len(cfgs) != len(meshes) or not meshes:
+        raise ValueError("one config per mesh is needed")
+    mh = (C.c_void_p * len(meshes))(*[m.h.value if isinstance(m.h, C.c_void_p) else m.h for m in meshes])
+    ca = (_lib.Config * len(cfgs))(*cfgs)
+    return mh, ca
+
+
+def batch_footprint(meshes, cfgs, precision="fp64"):
+    """Device bytes an arena of these solves takes (host-side layout only, no GPU)."""
+    mh, ca = _mesh_cfg_arrays(meshes, cfgs)
+    out = C.c_size_t()
+    err = C.create_string_buffer(512)
+    _check(_lib.load().ebb_batch_footprint(len(meshes), mh, ca, PRECISION[precision], C.byref(out), err, 512),
+           err.value.decode())
+    return out.value
+
+
+STATUS_FIELDS = [f[0] for f in _lib.InstanceStatus._fields_]
+
+
+class UfvmBatch(UfvmSolver):
+    """Many independent solves (mesh + config each) in one device arena, advanced
+    together by the same kernel launches; every instance stops at its own tEnd, step
+    limit or residual drop, and a NaN halts only its own instance."""
+
+    def __init__(self, meshes, cfgs, precision="fp64"):
+        L = _lib.load()
+        mh, ca = _mesh_cfg_arrays(meshes, cfgs)
+        self.meshes = list(meshes)
+        self.cfg = ca[0]
+        self.n = len(meshes)
+        self.n_cells = sum(m.n_cells for m in meshes)
+        self.face_slots = sum(m.info.face_slots for m in meshes)
+        h = C.c_void_p()
+        err = C.create_string_buffer(512)
+        _check(L.ebb_batch_create(self.n, mh, ca, PRECISION[precision], C.byref(h), err, 512), err.value.decode())
+        self.h = h
+
+    def instance_state(self, k):
+        q = np.zeros((self.meshes[k].n_cells, 4))
+        self._raise(_lib.load().ebb_batch_get_state(self.h, int(k), _dp(q)))
+        return q
+
+    def set_instance_state(self, k, q):
+        q = np.ascontiguousarray(q, dtype=np.float64).reshape(self.meshes[k].n_cells, 4)
+        self._raise(_lib.load().ebb_batch_set_state(self.h, int(k), _dp(q)))
+
+    def launch(self, nsteps):
+        """enqueue nsteps iterations on the arena's stream without waiting"""
+        self._raise(_lib.load().ebb_launch_steps(self.h, int(nsteps)))
+
+    def sync(self):
+        self._raise(_lib.load().ebb_sync(self.h))
+
+
+RESULT_FIELDS = [f[0] for f in _lib.RequestResult._fields_]
+
+
+class EbbServer:
+    """Continuous-batching request loop (include/ebb_gb300.h ebb_server_*): submit solves
+    at any time, call tick() to run scheduling rounds, collect finished results."""
+
+    def __init__(self, precision="split", **options):
+        L = _lib.load()
+        o = _lib.ServerOptions()
+        L.ebb_server_options_defaults(C.byref(o))
+        o.precision = PRECISION[precision]
+        for k, v in options.items():
+            setattr(o, k, v)
+        h = C.c_void_p()
+        err = C.create_string_buffer(512)
+        _check(L.ebb_server_create(C.byref(o), C.byref(h), err, 512), err.value.decode())
+        self.h = h
+        self.options = o
+        self.n_cells = {}
+
+    def submit(self, mesh, cfg, max_steps=0, resid_drop=0.0):
+        i = C.c_int64()
+        _check(_lib.load().ebb_server_submit(self.h, mesh.h, C.byref(cfg), int(max_steps), float(resid_drop),
+                                             C.byref(i)))
+        self.n_cells[i.value] = mesh.n_cells
+        return i.value
+
+    def tick(self):
+        a = C.c_int32()
+        w = C.c_int32()
+        _check(_lib.load().ebb_server_tick(self.h, C.byref(a), C.byref(w)))
+        return a.value, w.value
+
+    def results(self):
+        out = []
+        buf = (_lib.RequestResult * 256)()
+        n = C.c_int32()
+        while True:
+            _check(_lib.load().ebb_server_results(self.h, buf, 256, C.byref(n)))
+            for k in range(n.value):
+                d = {f: getattr(buf[k], f) for f in RESULT_FIELDS}
+                d["resid"] = list(d["resid"])
+                d["msg"] = d["msg"].decode(errors="replace")
+                out.append(d)
+            if n.value < 256:
+                return out
+
+    def take_state(self, rid):
+        q = np.zeros((self.n_cells[rid], 4))
+        _check(_lib.load().ebb_server_take_state(self.h, int(rid), _dp(q)))
+        return q
+
+    def stats(self):
+        s = _lib.ServerStats()
+        _check(_lib.load().ebb_server_stats_get(self.h, C.byref(s)))
+        return {f[0]: getattr(s, f[0]) for f in _lib.ServerStats._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            _lib.load().ebb_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

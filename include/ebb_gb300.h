@@ -220,6 +220,113 @@ int ebb_get_stream(ebb_solver *s, void **stream);
    ms[3] step end.  The state is left as it was. */
 int ebb_profile_kernels(ebb_solver *s, int32_t n_rep, double *ms);
 
+/* ---- batched arena (no counterpart in the reference: its driver runs one mesh per
+   process) ----------------------------------------------------------------- */
+/* n independent solves, each a mesh + config as for ebb_solver_create, laid out in one
+   device arena and advanced together: each kernel of a stage is one launch over the
+   cells and faces of every instance.  The instances must agree on flux, integrator,
+   limiter, order, viscosity and MMS kind (EBB_ERR_CONFIG otherwise); meshes, boundary
+   data, Mach, Reynolds, CFL, dt and tEnd may differ.  The handle takes the ebb_solver
+   calls: ebb_set_state / ebb_get_state move the instances' states concatenated in
+   instance order (ebb_batch_status gives each instance's offset); ebb_run advances
+   every instance that is not done until all are done or max_steps have run, and
+   writes no records when n > 1.  Each instance stops by itself at its tEnd, its step
+   limit or its residual drop (ebb_batch_set_stop), or at its first NaN, which halts
+   that instance only.  ebb_get_time / ebb_set_time / ebb_load_solution act on
+   instance 0; ebb_residual, ebb_residual_device and ebb_step return EBB_ERR_ARG when
+   n > 1.  Every instance's results are bitwise those of its own single solve. */
+int ebb_batch_create(int32_t n, const ebb_mesh *const *meshes, const ebb_config *cfgs, int32_t precision,
+                     ebb_solver **out, char *err, size_t err_len);
+
+typedef struct ebb_instance_status {
+    int64_t cell_offset; /* first row of the instance in ebb_get_state / ebb_set_state arrays */
+    int64_t n_cells;
+    int64_t iterations;
+    double t, dt, cfl;
+    int32_t done;      /* stopped: tEnd, step limit, residual drop, or an error */
+    int32_t status;    /* EBB_OK, or the error that stopped it */
+    int64_t err_index; /* reference index (within the instance) of the failing edge or cell, or -1 */
+    double drag, lift, resid[4], rmax; /* of the latest iteration */
+    double resid_first;                /* residMax of the first iteration (-1 before it) */
+} ebb_instance_status;
+
+int ebb_batch_size(const ebb_solver *s, int32_t *n);
+/* status of instances first .. first+count-1 (one device-to-host copy) */
+int ebb_batch_status(ebb_solver *s, int32_t first, int32_t count, ebb_instance_status *out);
+/* Stop conditions of instance k (every instance for k < 0): tEnd; a step limit
+   (max_steps > 0: done after that many iterations); a residual drop (resid_drop > 0:
+   done once residMax <= resid_drop x the first iteration's residMax). */
+int ebb_batch_set_stop(ebb_solver *s, int32_t k, double t_end, int64_t max_steps, double resid_drop);
+/* state of instance k alone, q[n_cells_k][4] in that mesh's reference cell order */
+int ebb_batch_get_state(ebb_solver *s, int32_t k, double *q);
+int ebb_batch_set_state(ebb_solver *s, int32_t k, const double *q);
+/* Enqueue n_steps iterations on the handle's stream and return without waiting
+   (instances already done skip their work); ebb_batch_status or ebb_sync waits. */
+int ebb_launch_steps(ebb_solver *s, int64_t n_steps);
+int ebb_sync(ebb_solver *s);
+/* device bytes ebb_batch_create would allocate for these meshes, without a device */
+int ebb_batch_footprint(int32_t n, const ebb_mesh *const *meshes, const ebb_config *cfgs, int32_t precision,
+                        size_t *bytes, char *err, size_t err_len);
+
+/* ---- request server (no counterpart in the reference) ---------------------
+   A continuous-batching loop over batched arenas.  Submitted solves are laid out on
+   host threads; each scheduling round (ebb_server_tick) retires instances that have
+   stopped (tEnd, step limit, residual drop or an error) and keeps their final states
+   until fetched, frees arenas whose instances have all stopped, admits waiting
+   requests into new arenas while their device bytes fit the budget (oldest first,
+   grouped with waiting requests of the same physics and similar size), and advances
+   every arena on its own stream so that arenas overlap on the device.  A request's
+   results are bitwise those of solving it alone with the same stop conditions. */
+typedef struct ebb_server ebb_server;
+
+typedef struct ebb_server_options {
+    int32_t precision;     /* EBB_PREC_FP64 or EBB_PREC_SPLIT (default split) */
+    int32_t max_arenas;    /* arenas on the device at once (default 32) */
+    int32_t max_batch;     /* instances per arena at most (default 512) */
+    int32_t build_threads; /* host threads laying out submitted meshes (default 4) */
+    double tick_ms;        /* device time each arena is given per round (default 25 ms) */
+    double size_ratio;     /* cell counts grouped in one arena differ by at most this factor (default 4) */
+    int64_t arena_cells;   /* cells per arena at most (default 8M) */
+    uint64_t hbm_budget;   /* device bytes all arenas together may take (default 150e9) */
+} ebb_server_options;
+
+typedef struct ebb_request_result {
+    int64_t id;
+    int32_t status; /* EBB_OK, or the error that ended the solve */
+    int32_t done_reason; /* 0 error, 1 tEnd, 2 step limit, 3 residual drop */
+    int64_t err_index;
+    int64_t n_cells;
+    int64_t iterations;
+    double t, drag, lift, resid[4], resid_first;
+    double submit_s, admit_s, finish_s; /* server clock: seconds since ebb_server_create */
+    char msg[96];
+} ebb_request_result;
+
+typedef struct ebb_server_stats {
+    uint64_t bytes_in_use, bytes_peak;
+    int32_t arenas, waiting, building, reserved;
+    int64_t submitted, finished, cell_updates;
+} ebb_server_stats;
+
+void ebb_server_options_defaults(ebb_server_options *o);
+int ebb_server_create(const ebb_server_options *o, ebb_server **out, char *err, size_t err_len);
+/* Queue one solve: mesh and config are copied (the caller may free them on return);
+   it stops after max_steps iterations (> 0), at a residual drop (> 0: residMax <=
+   resid_drop x the first iteration's) or at the config's tEnd, whichever comes first.
+   Thread-safe against ebb_server_tick. */
+int ebb_server_submit(ebb_server *sv, const ebb_mesh *mesh, const ebb_config *cfg, int64_t max_steps,
+                      double resid_drop, int64_t *id);
+/* One scheduling round; *n_active / *n_waiting (may be NULL) count arenas on the
+   device and requests not yet admitted (including those still being laid out). */
+int ebb_server_tick(ebb_server *sv, int32_t *n_active, int32_t *n_waiting);
+/* Results of requests finished since the last call, up to cap; *n the count. */
+int ebb_server_results(ebb_server *sv, ebb_request_result *out, int32_t cap, int32_t *n);
+/* Final state of a finished request, q[n_cells][4] in its mesh's reference cell
+   order; the server then releases it.  EBB_ERR_ARG for an unknown or taken id. */
+int ebb_server_take_state(ebb_server *sv, int64_t id, double *q);
+int ebb_server_stats_get(ebb_server *sv, ebb_server_stats *st);
+void ebb_server_destroy(ebb_server *sv);
+
 /* ---- flux seam (source/flux.d) ------------------------------------------ */
 /* Batched device evaluation of rusanovFlux!4 / roeFlux!4 on host arrays:
    qL,qR[n][4], normal[n][2] -> F[n][4], s_max[n]. */

@@ -214,3 +214,56 @@ def test_solver_create_fails_loudly_without_gpu():
     assert ei.value.code == 10
     with pytest.raises(E.EbbError):
         E.roe_flux(np.ones(4), np.ones(4), [1.0, 0.0])
+
+
+def test_instance_status_layout_matches_header(tmp_path):
+    """ebb_instance_status as a C compiler lays it out from the header vs the binding."""
+    src = tmp_path / "layout.c"
+    names = [f[0] for f in _lib.InstanceStatus._fields_]
+    body = "".join('printf("%%zu ", offsetof(ebb_instance_status, %s));' % n for n in names)
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "ebb_gb300.h"\nint main(void){%s'
+                   'printf("%%zu\\n", sizeof(ebb_instance_status));return 0;}\n' % body)
+    exe = tmp_path / "layout"
+    import subprocess
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    want = [getattr(_lib.InstanceStatus, n).offset for n in names] + [C.sizeof(_lib.InstanceStatus)]
+    assert got == want
+
+
+def _bump(n, mach=0.5, seed=0, **kw):
+    m = meshgen.bump_channel(n, h=0.05, seed=seed).to_solver_mesh()
+    cfg = E.default_config()
+    q = [mach, 0, 1, 1]
+    E.set_boundaries(cfg, [("Inflow", "fullState", q), ("Outflow", "fullState", q), ("Wall", "inviscidWall", q)])
+    for k, v in kw.items():
+        setattr(cfg, k, v)
+    return m, cfg
+
+
+def test_batch_footprint_without_device():
+    a = _bump(1500, seed=1)
+    b = _bump(4000, mach=0.7, seed=2)
+    fa = E.batch_footprint([a[0]], [a[1]])
+    fb = E.batch_footprint([b[0]], [b[1]])
+    fab = E.batch_footprint([a[0], b[0]], [a[1], b[1]])
+    assert fa > 1500 * 500 and fb > fa
+    assert 0.9 * (fa + fb) < fab < 1.1 * (fa + fb)
+    assert E.batch_footprint([a[0]], [a[1]], "split") < fa
+    # per-cell bytes are flat in the mesh size
+    assert abs(fa / a[0].n_cells - fb / b[0].n_cells) < 0.25 * fa / a[0].n_cells
+    bad = E.default_config()
+    with pytest.raises(E.EbbError) as ei:
+        E.batch_footprint([a[0]], [bad])
+    assert ei.value.code == 5
+
+
+def test_batch_create_fails_loudly_without_gpu():
+    L = _lib.load()
+    n = C.c_int()
+    if L.ebb_device_count(C.byref(n)) == 0:
+        pytest.skip("a GPU is present; the no-device path is not reachable")
+    a = _bump(800)
+    with pytest.raises(E.EbbError) as ei:
+        E.UfvmBatch([a[0], a[0]], [a[1], a[1]])
+    assert ei.value.code == 10
