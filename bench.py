@@ -334,6 +334,197 @@ def run_plate(args):
     return out
 
 
+def bump_json(mach, cfl=0.3):
+    q = [mach, 0, 1, 1]
+    return json.dumps({"mesh": "bump.msh", "dt": 1e-4, "tEnd": 1e9, "flux": "roeFlux", "saveIter": -1,
+                       "plotIter": -1, "forceBoundary": "Wall", "integrator": "RK2_TVD", "limited": True, "CFL": cfl,
+                       "initialConditions": q,
+                       "boudaryConditions": [{"tag": "Inflow", "type": "fullState", "q": q},
+                                             {"tag": "Outflow", "type": "fullState", "q": q},
+                                             {"tag": "Wall", "type": "inviscidWall", "q": q}]})
+
+
+def cylinder_json(re, mach=0.2, cfl=0.3):
+    q = [mach, 0, 1, 1]
+    far = [{"tag": t, "type": "fullState", "q": q} for t in ("Inflow", "Outflow", "Top", "Bottom")]
+    return json.dumps({"mesh": "cyl.msh", "dt": 1e-4, "tEnd": 1e9, "flux": "roeFlux", "saveIter": -1,
+                       "plotIter": -1, "forceBoundary": "Cylinder", "integrator": "RK2_TVD", "limited": True,
+                       "CFL": cfl, "viscosity": True, "initialConditions": q,
+                       "physicalConfig": {"Pr": 0.72, "R": 1.0, "gamma": 1.4, "Re": re, "L": 1.0},
+                       "boudaryConditions": far + [{"tag": "Cylinder", "type": "viscidWall", "q": q}]})
+
+
+def _gen_mesh(job):
+    kind, n, h, seed = job
+    from ebbcfd_gb300 import meshgen
+    return meshgen.bump_channel(n, h=h, seed=seed) if kind == "bump" else meshgen.cylinder(n, seed=seed)
+
+
+def gen_meshes(jobs):
+    """Seeded meshes generated on all host cores (spawned workers, no GPU state)."""
+    import multiprocessing as mp
+    with mp.get_context("spawn").Pool(max(1, min(len(jobs), os.cpu_count() or 1))) as pool:
+        return pool.map(_gen_mesh, jobs, chunksize=1)
+
+
+def seq_ms_per_step(L, E, meshes, cfgs, precision, steps, warmup):
+    """Device ms per step of each solve run alone (one solver at a time)."""
+    import ctypes as C
+    out = []
+    for m, c in zip(meshes, cfgs):
+        s = E.UfvmSolver(m, c, precision)
+        s.run(warmup, records=False)
+        n = C.c_int64()
+        ms = C.c_double()
+        code = L.ebb_run_timed(s.h, steps, C.byref(n), C.byref(ms))
+        if code:
+            s._raise(code)
+        out.append(ms.value / max(1, n.value))
+        s.close()
+    return out
+
+
+def run_batch512(args):
+    """512 independent Euler bump-channel solves in one arena: channel [0,3]x[0,1], bump
+    h sin^2(pi(x-1)) with h ~ U[0.02,0.1], seeded-Delaunay meshes with cell counts
+    log-uniform in [2e3, 2e5], Mach ~ U[0.3,0.8], split precision, Roe, TVD-RK2, 2000
+    steps each, against the same solves run one by one."""
+    import ctypes as C
+    import ebbcfd_gb300 as E
+    from ebbcfd_gb300 import _lib
+    n = args.instances
+    rng = np.random.default_rng(4)
+    cells = np.exp(rng.uniform(np.log(2e3), np.log(2e5), n)).astype(int)
+    hs = rng.uniform(0.02, 0.1, n)
+    machs = rng.uniform(0.3, 0.8, n)
+    steps = args.steps if args.steps_given else 2000
+    t0 = time.time()
+    gens = gen_meshes([("bump", int(c), float(h), k) for k, (c, h) in enumerate(zip(cells, hs))])
+    meshes = [g.to_solver_mesh() for g in gens]
+    mesh_s = time.time() - t0
+    cfgs = [E.load_config(bump_json(float(m))) for m in machs]
+    L = _lib.load()
+    ncell = int(sum(m.n_cells for m in meshes))
+    t0 = time.time()
+    b = E.UfvmBatch(meshes, cfgs, "split")
+    create_s = time.time() - t0
+    b.run(args.warmup, records=False)
+    kms = (C.c_double * 4)()
+    L.ebb_profile_kernels(b.h, 10, kms)
+    it0 = [s["iterations"] for s in b.status()]
+    clocks = Clocks(0)
+    clocks.start()
+    nrun = C.c_int64()
+    ms = C.c_double()
+    t0 = time.perf_counter()
+    code = L.ebb_run_timed(b.h, steps, C.byref(nrun), C.byref(ms))
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    if code:
+        b._raise(code)
+    st = b.status()
+    failed = [k for k, x in enumerate(st) if x["status"] != 0]
+    done_cu = sum(meshes[k].n_cells * (x["iterations"] - it0[k]) for k, x in enumerate(st))
+    value = done_cu / (ms.value / 1e3)
+    b.close()
+    # the same solves one by one: device time per step of each, on a sample of every
+    # stride-th instance, scaled to all instances and to the batch's step count
+    stride = max(1, args.seq_stride)
+    idx = list(range(0, n, stride))
+    seq = {}
+    for prec in ("split", "fp64"):
+        per = seq_ms_per_step(L, E, [meshes[i] for i in idx], [cfgs[i] for i in idx], prec, args.seq_steps,
+                              args.warmup)
+        est_ms = sum(per) * (n / len(idx)) * steps
+        cells_s = sum(meshes[i].n_cells for i in idx) * (n / len(idx)) * steps / (est_ms / 1e3)
+        seq[prec] = {"cell_updates_per_s": cells_s, "est_total_s": est_ms / 1e3}
+    peak, peak_kind = peaks()
+    return {"workload": "batch512-bump-roe-tvd-split", "instances": n, "cells": ncell, "steps": nrun.value,
+            "cell_updates_per_s": value, "cell_updates": done_cu, "instances_failed": len(failed),
+            "failed": [{"k": k, "cells": meshes[k].n_cells, "h": round(float(hs[k]), 4), "mach": round(float(machs[k]), 4),
+                        "status": st[k]["status"], "iterations": st[k]["iterations"]} for k in failed],
+            "device_s": ms.value / 1e3, "wall_s": wall, "mesh_s": round(mesh_s, 1),
+            "create_s": round(create_s, 2), "kernel_ms": list(kms), "clocks": clk,
+            "cells_min_max": [int(min(m.n_cells for m in meshes)), int(max(m.n_cells for m in meshes))],
+            "one_by_one": seq, "speedup_vs_one_by_one_split": value / seq["split"]["cell_updates_per_s"],
+            "speedup_vs_one_by_one_fp64": value / seq["fp64"]["cell_updates_per_s"],
+            "one_by_one_sample": "every %d-th instance (%d of %d), %d timed steps each after %d warm-up, scaled"
+                                 % (stride, len(idx), n, args.seq_steps, args.warmup), "hbm_peak_gbs": peak,
+            "peak_source": peak_kind}
+
+
+def run_serve(args):
+    """Served request stream: Poisson arrivals (seed 7, mean 40 req/s); 70% Euler bump
+    channels, 30% Navier-Stokes cylinders (Re ~ U[50,200], Mach 0.2); cell counts
+    log-uniform in [1e3, 2e6]; each stops at a 1e-8 residual drop or its step cap;
+    split precision; admission capped at 150 GB.  Latency = result in hand minus
+    scheduled arrival.  The sequential baseline is plain FP64 solves one at a time:
+    each request's device time per step alone (timed on a sample of steps) times the
+    steps it ran."""
+    import ebbcfd_gb300 as E
+    from ebbcfd_gb300 import _lib
+    R = args.requests
+    rng = np.random.default_rng(7)
+    arrivals = np.cumsum(rng.exponential(1.0 / 40.0, R))
+    kinds = np.where(rng.uniform(0, 1, R) < 0.7, "bump", "cyl")
+    cells = np.exp(rng.uniform(np.log(1e3), np.log(args.max_cells), R)).astype(int)
+    hs = rng.uniform(0.02, 0.1, R)
+    machs = rng.uniform(0.3, 0.8, R)
+    res = rng.uniform(50, 200, R)
+    cap = args.step_cap
+    t0 = time.time()
+    gens = gen_meshes([(str(k), int(c), float(h), i) for i, (k, c, h) in enumerate(zip(kinds, cells, hs))])
+    meshes = [g.to_solver_mesh() for g in gens]
+    mesh_s = time.time() - t0
+    cfgs = [E.load_config(bump_json(float(m)) if k == "bump" else cylinder_json(float(r)))
+            for k, m, r in zip(kinds, machs, res)]
+    L = _lib.load()
+    sv = E.EbbServer("split", hbm_budget=int(150e9), build_threads=8)
+    clocks = Clocks(0)
+    clocks.start()
+    tb = time.perf_counter()
+    nxt = 0
+    ids = {}
+    done = {}
+    while len(done) < R:
+        now = time.perf_counter() - tb
+        while nxt < R and arrivals[nxt] <= now:
+            ids[sv.submit(meshes[nxt], cfgs[nxt], cap, 1e-8)] = nxt
+            nxt += 1
+        a, w = sv.tick()
+        for r in sv.results():
+            k = ids[r["id"]]
+            r["latency_s"] = time.perf_counter() - tb - arrivals[k]
+            done[k] = r
+            if r["status"] == 0:
+                sv.take_state(r["id"])
+        if a == 0:
+            time.sleep(0.001)
+    wall = time.perf_counter() - tb
+    clk = clocks.stop()
+    stats = sv.stats()
+    sv.close()
+    lat = np.array([done[k]["latency_s"] for k in range(R)])
+    iters = np.array([done[k]["iterations"] for k in range(R)])
+    cu = float(sum(iters[k] * meshes[k].n_cells for k in range(R)))
+    # sequential plain FP64: per-step device time alone x steps run
+    per = seq_ms_per_step(L, E, meshes, cfgs, "fp64", args.seq_steps, 3)
+    seq_s = float(sum(per[k] * iters[k] for k in range(R)) / 1e3)
+    return {"workload": "served-bump70-cyl30-split", "requests": R, "arrival_rate_per_s": 40.0,
+            "cells_range": [int(cells.min()), int(cells.max())], "cells_total": int(sum(m.n_cells for m in meshes)),
+            "step_cap": cap, "resid_drop": 1e-8, "wall_s": wall, "solves_per_s": R / wall,
+            "cell_updates_per_s": cu / wall, "latency_p50_s": float(np.percentile(lat, 50)),
+            "latency_p99_s": float(np.percentile(lat, 99)), "latency_max_s": float(lat.max()),
+            "statuses": sorted(set(int(done[k]["status"]) for k in range(R))),
+            "done_reasons": {str(v): int((np.array([done[k]["done_reason"] for k in range(R)]) == v).sum())
+                             for v in (0, 1, 2, 3)},
+            "sequential_fp64": {"est_total_s": seq_s, "cell_updates_per_s": cu / seq_s,
+                                "sample": "%d timed steps per request alone after 3 warm-up, x steps run"
+                                          % args.seq_steps},
+            "throughput_vs_sequential_fp64": (cu / wall) / (cu / seq_s), "bytes_peak": stats["bytes_peak"],
+            "mesh_s": round(mesh_s, 1), "clocks": clk}
+
+
 def run_reference(args, ws, rank):
     from ebbcfd_gb300 import meshgen
     from oracle import gmsh_ref, ref
@@ -373,7 +564,13 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-split", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
-    ap.add_argument("--workload", default="wedge", choices=["wedge", "mms32", "plate4m"])
+    ap.add_argument("--workload", default="wedge", choices=["wedge", "mms32", "plate4m", "batch512", "serve"])
+    ap.add_argument("--instances", type=int, default=512)
+    ap.add_argument("--seq-stride", type=int, default=4)
+    ap.add_argument("--seq-steps", type=int, default=100)
+    ap.add_argument("--requests", type=int, default=32)
+    ap.add_argument("--max-cells", type=float, default=2e6)
+    ap.add_argument("--step-cap", type=int, default=50000)
     args = ap.parse_args()
     args.steps_given = "--steps" in sys.argv
     args.cells_given = "--cells" in sys.argv
@@ -381,7 +578,8 @@ def main():
     ws, rank, local = dist_env()
     if args.workload != "wedge":
         # accuracy/throughput reports for the other configurations (not the headline line)
-        out = run_mms32(args) if args.workload == "mms32" else run_plate(args)
+        run = {"mms32": run_mms32, "plate4m": run_plate, "batch512": run_batch512, "serve": run_serve}
+        out = run[args.workload](args)
         print(json.dumps(out))
         return
     if args.impl == "reference":

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <thread>
 
 #include "solver_impl.hpp"
 
@@ -286,15 +287,27 @@ int ebb_batch_create(int32_t n, const ebb_mesh *const *meshes, const ebb_config 
         set_err(err, err_len, "no CUDA device available");
         return EBB_ERR_NO_DEVICE;
     }
+    // host layouts of the instances, built in parallel (independent meshes)
     std::vector<InstLayout> Ls(n);
-    std::string e;
-    for (int32_t k = 0; k < n; k++) {
-        int r = build_instance(meshes[k], &cfgs[k], Ls[k], e);
-        if (r) {
-            set_err(err, err_len, n > 1 ? "instance " + std::to_string(k) + ": " + e : e);
-            return r;
-        }
+    std::vector<int> rc(n, EBB_OK);
+    std::vector<std::string> msg(n);
+    const int nt = (int)std::min<unsigned>((unsigned)n, std::max(1u, std::thread::hardware_concurrency()));
+    auto work = [&](int t0) {
+        for (int32_t k = t0; k < n; k += nt) rc[k] = build_instance(meshes[k], &cfgs[k], Ls[k], msg[k]);
+    };
+    if (nt == 1) {
+        work(0);
+    } else {
+        std::vector<std::thread> th;
+        for (int t = 0; t < nt; t++) th.emplace_back(work, t);
+        for (auto &x : th) x.join();
     }
+    for (int32_t k = 0; k < n; k++)
+        if (rc[k]) {
+            set_err(err, err_len, n > 1 ? "instance " + std::to_string(k) + ": " + msg[k] : msg[k]);
+            return rc[k];
+        }
+    std::string e;
     auto *s = new ebb_solver();
     int r = assemble(s, Ls, precision, e);
     if (r) {

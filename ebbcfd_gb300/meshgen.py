@@ -241,8 +241,15 @@ def bump_channel(n_cells=20000, h=0.05, seed=0):
     ip = _interior_points(rng, 0, 3, 0, 1, lambda x, y: np.full(np.shape(x), hc), inside, hc)
     nodes = np.vstack([bpts, ip])
     tri = Delaunay(nodes).simplices.astype(np.int64)
+    # the convex hull also covers the region under the bump: drop those triangles
+    c = nodes[tri].mean(axis=1)
+    tri = tri[c[:, 1] > floor_y(c[:, 0])]
     tris, a = _ccw(nodes, tri)
     tris = tris[a > 1e-14]
+    used = np.unique(tris)
+    remap = np.full(len(nodes), -1, np.int64)
+    remap[used] = np.arange(len(used))
+    nodes, tris = nodes[used], remap[tris]
     tags = ["Inflow", "Outflow", "Wall"]
     eps = 1e-9
 

@@ -1,0 +1,126 @@
+"""Request server: solves submitted while others run are admitted into arenas as
+memory frees up, overlap on the device, and each result is bitwise the result of
+solving that request alone with the same stop conditions."""
+import json
+
+import numpy as np
+import pytest
+
+import ebbcfd_gb300 as E
+from ebbcfd_gb300 import meshgen
+
+pytestmark = pytest.mark.gpu
+
+
+def bump_cfg(mach):
+    q = [mach, 0, 1, 1]
+    return E.load_config(json.dumps({
+        "mesh": "m.msh", "dt": 1e-4, "tEnd": 1000.0, "flux": "roeFlux", "saveIter": -1, "plotIter": -1,
+        "forceBoundary": "Wall", "initialConditions": q, "integrator": "RK2_TVD", "CFL": 0.5,
+        "boudaryConditions": [{"tag": "Inflow", "type": "fullState", "q": q},
+                              {"tag": "Outflow", "type": "fullState", "q": q},
+                              {"tag": "Wall", "type": "inviscidWall", "q": q}]}))
+
+
+def cylinder_cfg(re, mach=0.2):
+    q = [mach, 0, 1, 1]
+    far = [{"tag": t, "type": "fullState", "q": q} for t in ("Inflow", "Outflow", "Top", "Bottom")]
+    return E.load_config(json.dumps({
+        "mesh": "m.msh", "dt": 1e-4, "tEnd": 1000.0, "flux": "roeFlux", "saveIter": -1, "plotIter": -1,
+        "forceBoundary": "Cylinder", "initialConditions": q, "integrator": "RK2_TVD", "CFL": 0.5,
+        "viscosity": True, "physicalConfig": {"Pr": 0.72, "R": 1.0, "gamma": 1.4, "Re": re, "L": 1.0},
+        "boudaryConditions": far + [{"tag": "Cylinder", "type": "viscidWall", "q": q}]}))
+
+
+@pytest.fixture(scope="module")
+def requests():
+    out = []
+    for k, (kind, n, p, steps) in enumerate([("bump", 800, 0.3, 40), ("bump", 3000, 0.5, 64),
+                                              ("cyl", 1000, 80.0, 33), ("bump", 1500, 0.7, 50),
+                                              ("cyl", 3000, 150.0, 48), ("bump", 6000, 0.8, 70),
+                                              ("bump", 2500, 0.6, 0)]):
+        if kind == "bump":
+            m, c = meshgen.bump_channel(n, h=0.05, seed=k).to_solver_mesh(), bump_cfg(p)
+        else:
+            m, c = meshgen.cylinder(n, seed=k).to_solver_mesh(), cylinder_cfg(p)
+        out.append((m, c, steps))
+    return out
+
+
+def solo(mesh, cfg, max_steps, resid_drop, precision):
+    s = E.UfvmSolver(mesh, cfg, precision)
+    s.set_stop(0, t_end=cfg.t_end, max_steps=max_steps, resid_drop=resid_drop)
+    s.run(10 ** 6, records=False)
+    out = s.state, s.status()[0]
+    s.close()
+    return out
+
+
+def serve(requests, precision, **opts):
+    sv = E.EbbServer(precision, **opts)
+    ids = {}
+    drop = 0.5  # the request without a step limit stops at a residual drop
+    for k, (m, c, steps) in enumerate(requests[:3]):
+        ids[sv.submit(m, c, steps, 0.0 if steps else drop)] = k
+    results = {}
+    for _ in range(3):
+        sv.tick()
+    for k, (m, c, steps) in enumerate(requests[3:], start=3):
+        ids[sv.submit(m, c, steps, 0.0 if steps else drop)] = k
+    for _ in range(100000):
+        a, w = sv.tick()
+        for r in sv.results():
+            results[ids[r["id"]]] = (r, sv.take_state(r["id"]))
+        if len(results) == len(requests) and a == 0 and w == 0:
+            break
+    stats = sv.stats()
+    sv.close()
+    return results, stats, drop
+
+
+@pytest.mark.parametrize("precision", ["split", "fp64"])
+def test_served_results_equal_solo_solves(requests, precision):
+    results, stats, drop = serve(requests, precision, max_batch=3, tick_ms=1.0, build_threads=2)
+    assert len(results) == len(requests)
+    assert stats["finished"] == len(requests) and stats["bytes_in_use"] == 0
+    for k, (m, c, steps) in enumerate(requests):
+        r, q = results[k]
+        assert r["status"] == 0, r
+        qs, st = solo(m, c, steps, 0.0 if steps else drop, precision)
+        assert np.array_equal(q, qs), (k, np.abs(q - qs).max())
+        assert r["iterations"] == st["iterations"] and r["t"] == st["t"]
+        assert r["drag"] == st["drag"] and r["lift"] == st["lift"]
+        assert r["done_reason"] == (2 if steps else 3)
+        assert r["submit_s"] <= r["admit_s"] <= r["finish_s"]
+    assert stats["cell_updates"] == sum(results[k][0]["iterations"] * m.n_cells
+                                        for k, (m, _, _) in enumerate(requests))
+
+
+def test_admission_respects_the_device_budget(requests):
+    one = max(E.batch_footprint([m], [c], "split") for m, c, _ in requests)
+    results, stats, _ = serve(requests, "split", hbm_budget=int(1.5 * one), tick_ms=1.0)
+    assert len(results) == len(requests) and all(r["status"] == 0 for r, _ in results.values())
+    assert 0 < stats["bytes_peak"] <= int(1.5 * one)
+    admits = sorted(r["admit_s"] for r, _ in results.values())
+    assert admits[-1] > admits[0]  # later requests waited for memory
+
+
+def test_failed_requests_are_reported(requests):
+    m, c, _ = requests[0]
+    bad = bump_cfg(0.5)
+    bad.n_boundaries = 2  # the Wall tag has no condition
+    sv = E.EbbServer("split")
+    i_bad = sv.submit(m, bad, 10)
+    i_ok = sv.submit(m, c, 10)
+    got = {}
+    for _ in range(10000):
+        a, w = sv.tick()
+        for r in sv.results():
+            got[r["id"]] = r
+        if len(got) == 2 and a == 0 and w == 0:
+            break
+    assert got[i_bad]["status"] == 5 and "Wall" in got[i_bad]["msg"]
+    assert got[i_ok]["status"] == 0 and got[i_ok]["iterations"] == 10
+    with pytest.raises(E.EbbError):
+        sv.take_state(i_bad)
+    sv.close()

@@ -267,3 +267,38 @@ def test_batch_create_fails_loudly_without_gpu():
     with pytest.raises(E.EbbError) as ei:
         E.UfvmBatch([a[0], a[0]], [a[1], a[1]])
     assert ei.value.code == 10
+
+
+def test_server_create_fails_loudly_without_gpu():
+    L = _lib.load()
+    n = C.c_int()
+    if L.ebb_device_count(C.byref(n)) == 0:
+        pytest.skip("a GPU is present; the no-device path is not reachable")
+    with pytest.raises(E.EbbError) as ei:
+        E.EbbServer("split")
+    assert ei.value.code == 10
+
+
+def test_cylinder_generator():
+    g = meshgen.cylinder(5000, seed=3)
+    m = g.to_solver_mesh()
+    assert 0.8 * 5000 < m.n_cells < 1.25 * 5000
+    assert m.tags == ["Inflow", "Outflow", "Top", "Bottom", "Cylinder"]
+    xy = m.centroids()
+    assert (np.hypot(xy[:, 0], xy[:, 1]) > 0.5).all()
+    assert xy[:, 0].min() > -10 and xy[:, 0].max() < 30 and np.abs(xy[:, 1]).max() < 10
+
+
+def test_bump_channel_mesh_follows_the_bump():
+    """No triangle of the channel lies under the bump (the Delaunay hull covers that
+    region) and no sliver survives."""
+    h = 0.1
+    g = meshgen.bump_channel(6000, h=h, seed=212)
+    tr = np.asarray(g.elements) - 1
+    p = g.nodes[tr]
+    c = p.mean(axis=1)
+    floor = np.where((c[:, 0] >= 1) & (c[:, 0] <= 2), h * np.sin(np.pi * (c[:, 0] - 1)) ** 2, 0.0)
+    assert (c[:, 1] > floor).all()
+    a = 0.5 * ((p[:, 1, 0] - p[:, 0, 0]) * (p[:, 2, 1] - p[:, 0, 1]) - (p[:, 2, 0] - p[:, 0, 0]) * (p[:, 1, 1] - p[:, 0, 1]))
+    l2 = ((p[:, 1] - p[:, 0]) ** 2).sum(1) + ((p[:, 2] - p[:, 1]) ** 2).sum(1) + ((p[:, 0] - p[:, 2]) ** 2).sum(1)
+    assert (4 * np.sqrt(3) * a / l2).min() > 0.1
