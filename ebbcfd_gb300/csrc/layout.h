@@ -75,8 +75,8 @@ struct DState {
     int32_t rec_enabled;
     float dtf, dt_half_f, dt_sixth_f;  // FP32 copies for the split path's increments
     int64_t max_steps;                 // > 0: done after this many iterations
-    double stop_drop;                  // > 0: done once residMax <= stop_drop * first residMax
-    double resid_first;                // residMax of the first iteration (< 0: not yet seen)
+    double stop_drop;                  // > 0: done once the density residual <= stop_drop * its first value
+    double resid_first;                // density residual of the first iteration (< 0: not yet seen)
     double last[7];                    // drag, lift, resid[4], Rmax of the latest iteration
 };
 

@@ -247,7 +247,7 @@ typedef struct ebb_instance_status {
     int32_t status;    /* EBB_OK, or the error that stopped it */
     int64_t err_index; /* reference index (within the instance) of the failing edge or cell, or -1 */
     double drag, lift, resid[4], rmax; /* of the latest iteration */
-    double resid_first;                /* residMax of the first iteration (-1 before it) */
+    double resid_first;                /* density residual of the first iteration (-1 before it) */
 } ebb_instance_status;
 
 int ebb_batch_size(const ebb_solver *s, int32_t *n);
@@ -255,7 +255,8 @@ int ebb_batch_size(const ebb_solver *s, int32_t *n);
 int ebb_batch_status(ebb_solver *s, int32_t first, int32_t count, ebb_instance_status *out);
 /* Stop conditions of instance k (every instance for k < 0): tEnd; a step limit
    (max_steps > 0: done after that many iterations); a residual drop (resid_drop > 0:
-   done once residMax <= resid_drop x the first iteration's residMax). */
+   done once the density residual resid[0] <= resid_drop x its first-iteration value;
+   the density residual is the one of the four whose normalising sum cannot vanish). */
 int ebb_batch_set_stop(ebb_solver *s, int32_t k, double t_end, int64_t max_steps, double resid_drop);
 /* state of instance k alone, q[n_cells_k][4] in that mesh's reference cell order */
 int ebb_batch_get_state(ebb_solver *s, int32_t k, double *q);
@@ -311,8 +312,8 @@ typedef struct ebb_server_stats {
 void ebb_server_options_defaults(ebb_server_options *o);
 int ebb_server_create(const ebb_server_options *o, ebb_server **out, char *err, size_t err_len);
 /* Queue one solve: mesh and config are copied (the caller may free them on return);
-   it stops after max_steps iterations (> 0), at a residual drop (> 0: residMax <=
-   resid_drop x the first iteration's) or at the config's tEnd, whichever comes first.
+   it stops after max_steps iterations (> 0), at a residual drop (> 0: density residual
+   <= resid_drop x its first-iteration value) or at the config's tEnd, whichever first.
    Thread-safe against ebb_server_tick. */
 int ebb_server_submit(ebb_server *sv, const ebb_mesh *mesh, const ebb_config *cfg, int64_t max_steps,
                       double resid_drop, int64_t *id);
