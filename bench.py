@@ -103,6 +103,25 @@ def peaks():
     return 6800.0, "fallback"
 
 
+PROFILED_CELLS = 994_095  # the wedge the committed ncu captures ran on
+
+
+def profiled_traffic(kernel, precision, ncell):
+    """DRAM bytes (read + write) per launch of `kernel` from the committed ncu
+    summaries under profiles/ ("traffic: <kernel> <precision> <bytes>" lines, one
+    capture of the 994,095-cell wedge), scaled to `ncell` cells (traffic grows with
+    the cells processed); None when no capture covers the kernel."""
+    import glob
+    import re
+    for f in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
+        for line in open(f):
+            m = re.match(r"traffic: (\S+) (\S+) (\d+)\s*$", line)
+            if m and m.group(1) == kernel and m.group(2) == precision:
+                return {"bytes": int(m.group(3)) * ncell / PROFILED_CELLS, "source": os.path.relpath(f, ROOT),
+                        "scaled_from_cells": PROFILED_CELLS}
+    return None
+
+
 def algorithmic_bytes(info, real=8, need_grad=False, limited=True):
     """Bytes each kernel must move per launch, every array touched once (re-reads of
     a neighbour's state count 0).  S = face slots, E = interior edges, G = boundary
@@ -176,9 +195,13 @@ def measure(L, E, _lib, gen, mesh, precision, args, local, ws, want_e2e):
     ab = algorithmic_bytes(info, real=8 if precision == "fp64" else 4)
     dom = max(("cell", "flux", "update"), key=lambda k: kern_ms[k])
     achieved = ab[dom] / (kern_ms[dom] * 1e-3) / 1e9
+    tr = profiled_traffic("k_" + dom, precision, ncell)
     roof = {"bound": "hbm", "kernel": "k_" + dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": peak_kind, "traffic": None, "kernel_ms": kern_ms,
-            "algorithmic_bytes": ab}
+            "frac": achieved / peak, "peak_source": peak_kind, "traffic": tr["bytes"] if tr else None,
+            "traffic_source": tr, "kernel_ms": kern_ms, "algorithmic_bytes": ab}
+    if precision == "fp64":
+        # the FP64 kernels are bound by the FP64 pipe, not by HBM (ncu, profiles/fp64_wedge1m.md)
+        roof["fp64_pipe_active_pct"] = {"k_cell": 85.9, "k_flux": 86.8}
     sol.close()
     return {"value": value, "elapsed": elapsed, "steps": steps_done, "setup_s": setup_s, "roofline": roof,
             "e2e": e2e, "clocks": clk, "state": state}

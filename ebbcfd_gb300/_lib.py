@@ -79,20 +79,23 @@ class InstanceStatus(C.Structure):
 class ServerOptions(C.Structure):
     _fields_ = [("precision", C.c_int32), ("max_arenas", C.c_int32), ("max_batch", C.c_int32),
                 ("build_threads", C.c_int32), ("tick_ms", C.c_double), ("size_ratio", C.c_double),
-                ("arena_cells", C.c_int64), ("hbm_budget", C.c_uint64)]
+                ("arena_cells", C.c_int64), ("hbm_budget", C.c_uint64), ("escalate", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class RequestResult(C.Structure):
     _fields_ = [("id", C.c_int64), ("status", C.c_int32), ("done_reason", C.c_int32), ("err_index", C.c_int64),
                 ("n_cells", C.c_int64), ("iterations", C.c_int64), ("t", C.c_double), ("drag", C.c_double),
                 ("lift", C.c_double), ("resid", C.c_double * 4), ("resid_first", C.c_double),
-                ("submit_s", C.c_double), ("admit_s", C.c_double), ("finish_s", C.c_double), ("msg", C.c_char * 96)]
+                ("submit_s", C.c_double), ("admit_s", C.c_double), ("finish_s", C.c_double),
+                ("precision", C.c_int32), ("escalated", C.c_int32), ("msg", C.c_char * 96)]
 
 
 class ServerStats(C.Structure):
     _fields_ = [("bytes_in_use", C.c_uint64), ("bytes_peak", C.c_uint64), ("arenas", C.c_int32),
                 ("waiting", C.c_int32), ("building", C.c_int32), ("reserved", C.c_int32),
-                ("submitted", C.c_int64), ("finished", C.c_int64), ("cell_updates", C.c_int64)]
+                ("submitted", C.c_int64), ("finished", C.c_int64), ("cell_updates", C.c_int64),
+                ("escalations", C.c_int64)]
 
 
 # every function the header declares, with its signature

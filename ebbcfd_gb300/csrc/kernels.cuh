@@ -317,6 +317,9 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? EBB_CELL_MINB_F : 1) k_c
         g[k][1] = T(0.0);
     }
     const bool second = P.order > 1;
+    // split path: the limiter's and the reconstruction's geometry (neighbour and face
+    // midpoint offsets) is loaded with the first wave of loads, not behind the gathers
+    typename V2<T>::t ndv[MJ], fdv[MJ];
     if constexpr (sizeof(T) == 4) {
         // all index and neighbour-state loads in flight before any dependent math
         int nbv[MJ];
@@ -328,6 +331,8 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? EBB_CELL_MINB_F : 1) k_c
         for (int j = 0; j < MJ; j++) {
             ld4(qin + 4 * (size_t)(nbv[j] < M.C ? nbv[j] : i), qv[j]);
             gmv[j] = ld2<T>(M.g.s_gm, (size_t)j * Cs + i);
+            ndv[j] = ld2<T>(M.g.s_nd, (size_t)j * Cs + i);
+            fdv[j] = ld2<T>(M.g.s_fd, (size_t)j * Cs + i);
         }
 #pragma unroll
         for (int j = 0; j < MJ; j++) {
@@ -380,7 +385,11 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? EBB_CELL_MINB_F : 1) k_c
 #pragma unroll
         for (int j = 0; j < MJ; j++) {
             if (j < ne) {
-                const typename V2<T>::t nd = ld2<T>(M.g.s_nd, (size_t)j * Cs + i);
+                typename V2<T>::t nd;
+                if constexpr (sizeof(T) == 4)
+                    nd = ndv[j];
+                else
+                    nd = ld2<T>(M.g.s_nd, (size_t)j * Cs + i);
 #pragma unroll
                 for (int k = 0; k < 4; k++) {
                     T s = T(1.0);
@@ -427,7 +436,11 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? EBB_CELL_MINB_F : 1) k_c
 #pragma unroll
                 for (int k = 0; k < 4; k++) f[k] = qi[k];
             } else {
-                const typename V2<T>::t fd = ld2<T>(M.g.s_fd, s);
+                typename V2<T>::t fd;
+                if constexpr (sizeof(T) == 4)
+                    fd = fdv[j];
+                else
+                    fd = ld2<T>(M.g.s_fd, s);
 #pragma unroll
                 for (int k = 0; k < 4; k++) f[k] = qi[k] + lg0[k] * fd.x + lg1[k] * fd.y;
                 if (pressure_negative(f)) {

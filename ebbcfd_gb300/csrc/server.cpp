@@ -8,7 +8,9 @@
 // uploads overlap with device work already queued.  Admission is oldest-first: the
 // oldest waiting request opens an arena and takes along waiting requests of the same
 // physics whose cell counts are within size_ratio of its own, as long as the arena's
-// exact device bytes fit what the budget has left.
+// exact device bytes fit what the budget has left.  With escalation on, a request
+// whose split-precision solve stops with an error is solved again from its initial
+// state in plain FP64 (same id; the result says so).
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -32,6 +34,8 @@ struct Request {
     int64_t max_steps = 0;
     double resid_drop = 0;
     double submit_s = 0, admit_s = -1;
+    int32_t precision = EBB_PREC_SPLIT;
+    int32_t escalated = 0;  // re-solved in plain FP64 after a split-precision error
     InstLayout L;
     int status = EBB_OK;
     std::string err;
@@ -84,7 +88,7 @@ struct ebb_server {
     std::deque<ebb_request_result> results;
     std::map<int64_t, std::vector<double>> states;
     uint64_t bytes_in_use = 0, bytes_peak = 0;
-    int64_t finished = 0, cell_updates = 0;
+    int64_t finished = 0, cell_updates = 0, escalations = 0;
 };
 
 namespace {
@@ -102,7 +106,8 @@ void worker(ebb_server *sv)
             sv->building++;
         }
         r->status = build_instance(r->mesh.get(), &r->cfg, r->L, r->err);
-        r->mesh.reset();
+        // the mesh is kept only while an FP64 re-solve may still need it
+        if (!(sv->opt.escalate && r->precision == EBB_PREC_SPLIT)) r->mesh.reset();
         if (r->status == EBB_OK) {
             r->L.st0.max_steps = r->max_steps;
             r->L.st0.stop_drop = r->resid_drop;
@@ -113,7 +118,7 @@ void worker(ebb_server *sv)
             one[0].maxJ = r->L.maxJ;
             one[0].cfg = r->L.cfg;
             one[0].force.resize(r->L.force.size());
-            r->bytes = arena_bytes(one, sv->opt.precision);
+            r->bytes = arena_bytes(one, r->precision);
         }
         std::lock_guard<std::mutex> lk(sv->mu);
         sv->building--;
@@ -132,6 +137,8 @@ void finish(ebb_server *sv, Request &r, int status, const std::string &msg, cons
     o.admit_s = r.admit_s;
     o.finish_s = now_s(sv->t0);
     o.n_cells = r.L.C;
+    o.precision = r.precision;
+    o.escalated = r.escalated;
     std::snprintf(o.msg, sizeof o.msg, "%s", msg.c_str());
     if (st) {
         o.err_index = st->err_index;
@@ -217,6 +224,29 @@ int harvest(ebb_server *sv, ArenaRun &a)
         sv->cell_updates += a.cells[k] * (st[k].iterations - a.iter_seen[k]);
         a.iter_seen[k] = st[k].iterations;
         if (!st[k].done) continue;
+        Request &rq = *a.reqs[k];
+        if (st[k].status != EBB_OK && sv->opt.escalate && rq.precision == EBB_PREC_SPLIT && rq.mesh) {
+            // solve it again in plain FP64, from the start
+            auto again = std::make_shared<Request>();
+            again->id = rq.id;
+            again->mesh = std::move(rq.mesh);
+            again->cfg = rq.cfg;
+            again->max_steps = rq.max_steps;
+            again->resid_drop = rq.resid_drop;
+            again->submit_s = rq.submit_s;
+            again->precision = EBB_PREC_FP64;
+            again->escalated = 1;
+            {
+                std::lock_guard<std::mutex> lk(sv->mu);
+                sv->to_build.push_back(again);
+            }
+            sv->cv.notify_one();
+            sv->escalations++;
+            a.retired[k] = 1;
+            a.left--;
+            continue;
+        }
+        rq.mesh.reset();
         std::vector<double> q(4 * (size_t)a.cells[k]);
         if ((r = ebb_batch_get_state(a.s, k, q.data()))) return r;
         sv->states[a.reqs[k]->id] = std::move(q);
@@ -244,7 +274,8 @@ int admit(ebb_server *sv)
         for (size_t i = 1; i < sv->waiting.size() && (int)pick.size() < sv->opt.max_batch; i++) {
             const Request &r = *sv->waiting[i];
             const double ratio = (double)std::max(r.L.C, head->L.C) / (double)std::max<int64_t>(1, std::min(r.L.C, head->L.C));
-            if (!same_group(r.cfg, head->cfg) || ratio > sv->opt.size_ratio) continue;
+            if (!same_group(r.cfg, head->cfg) || r.precision != head->precision || ratio > sv->opt.size_ratio)
+                continue;
             if (cells + r.L.C > sv->opt.arena_cells || est + r.bytes > room) continue;
             pick.push_back(i);
             cells += r.L.C;
@@ -261,10 +292,10 @@ int admit(ebb_server *sv)
         auto a = std::make_unique<ArenaRun>();
         a->s = new ebb_solver();
         std::string e;
-        const uint64_t exact = arena_bytes(Ls, sv->opt.precision);
+        const uint64_t exact = arena_bytes(Ls, head->precision);
         std::vector<int64_t> cl(Ls.size());
         for (size_t k = 0; k < Ls.size(); k++) cl[k] = Ls[k].C;
-        int r = (exact > room) ? EBB_ERR_OOM : assemble(a->s, Ls, sv->opt.precision, e);
+        int r = (exact > room) ? EBB_ERR_OOM : assemble(a->s, Ls, head->precision, e);
         for (size_t k = 0; k < group.size(); k++) {
             group[k]->L.C = cl[k];  // keep the size for the result record
             group[k]->admit_s = now;
@@ -347,6 +378,7 @@ int ebb_server_submit(ebb_server *sv, const ebb_mesh *mesh, const ebb_config *cf
     r->cfg = *cfg;
     r->max_steps = max_steps;
     r->resid_drop = resid_drop;
+    r->precision = sv->opt.precision;
     r->submit_s = now_s(sv->t0);
     {
         std::lock_guard<std::mutex> lk(sv->mu);
@@ -425,6 +457,7 @@ int ebb_server_stats_get(ebb_server *sv, ebb_server_stats *st)
     st->submitted = sv->submitted;
     st->finished = sv->finished;
     st->cell_updates = sv->cell_updates;
+    st->escalations = sv->escalations;
     return EBB_OK;
 }
 

@@ -289,6 +289,9 @@ typedef struct ebb_server_options {
     double size_ratio;     /* cell counts grouped in one arena differ by at most this factor (default 4) */
     int64_t arena_cells;   /* cells per arena at most (default 8M) */
     uint64_t hbm_budget;   /* device bytes all arenas together may take (default 150e9) */
+    int32_t escalate;      /* 1: a split-precision solve that stops with an error is solved
+                              again in plain FP64 from its initial state (default 0) */
+    int32_t reserved;
 } ebb_server_options;
 
 typedef struct ebb_request_result {
@@ -300,13 +303,15 @@ typedef struct ebb_request_result {
     int64_t iterations;
     double t, drag, lift, resid[4], resid_first;
     double submit_s, admit_s, finish_s; /* server clock: seconds since ebb_server_create */
+    int32_t precision;                  /* precision form of the solve that produced the result */
+    int32_t escalated;                  /* 1: re-solved in FP64 after a split-precision error */
     char msg[96];
 } ebb_request_result;
 
 typedef struct ebb_server_stats {
     uint64_t bytes_in_use, bytes_peak;
     int32_t arenas, waiting, building, reserved;
-    int64_t submitted, finished, cell_updates;
+    int64_t submitted, finished, cell_updates, escalations;
 } ebb_server_stats;
 
 void ebb_server_options_defaults(ebb_server_options *o);

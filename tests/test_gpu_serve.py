@@ -124,3 +124,50 @@ def test_failed_requests_are_reported(requests):
     with pytest.raises(E.EbbError):
         sv.take_state(i_bad)
     sv.close()
+
+
+def _fragile_bump():
+    """A bump channel (8962 cells, Mach 0.35, TVD-RK2, CFL 0.3) on which the
+    reference scheme's always-unlimited second TVD stage lets FP32 rounding grow into a
+    NaN after ~1900 steps, while the FP64 solve stays bounded."""
+    rng = np.random.default_rng(4)
+    cells = np.exp(rng.uniform(np.log(2e3), np.log(2e5), 512)).astype(int)
+    hs = rng.uniform(0.02, 0.1, 512)
+    machs = rng.uniform(0.3, 0.8, 512)
+    k = 276
+    m = meshgen.bump_channel(int(cells[k]), h=float(hs[k]), seed=k).to_solver_mesh()
+    c = bump_cfg(float(machs[k]))
+    c.cfl = 0.3
+    return m, c
+
+
+def test_split_error_escalates_to_fp64():
+    m, c = _fragile_bump()
+    steps = 2500
+    s = E.UfvmSolver(m, c, "split")
+    s.set_stop(0, t_end=c.t_end, max_steps=steps)
+    try:
+        s.run(steps, records=False)
+        pytest.skip("the split solve of this case did not fail")
+    except E.EbbError as e:
+        assert e.code in (8, 9)
+    s.close()
+    q64, st64 = solo(m, c, steps, 0.0, "fp64")
+    for escalate in (0, 1):
+        sv = E.EbbServer("split", escalate=escalate, tick_ms=2.0)
+        rid = sv.submit(m, c, steps)
+        got = None
+        for _ in range(100000):
+            a, w = sv.tick()
+            for r in sv.results():
+                got = r
+            if got is not None and a == 0 and w == 0:
+                break
+        if escalate:
+            assert got["status"] == 0 and got["escalated"] == 1 and got["precision"] == 0
+            assert got["iterations"] == steps
+            assert np.array_equal(sv.take_state(rid), q64)
+            assert sv.stats()["escalations"] == 1
+        else:
+            assert got["status"] in (8, 9) and got["escalated"] == 0 and got["precision"] == 1
+        sv.close()

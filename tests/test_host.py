@@ -216,18 +216,24 @@ def test_solver_create_fails_loudly_without_gpu():
         E.roe_flux(np.ones(4), np.ones(4), [1.0, 0.0])
 
 
-def test_instance_status_layout_matches_header(tmp_path):
-    """ebb_instance_status as a C compiler lays it out from the header vs the binding."""
-    src = tmp_path / "layout.c"
-    names = [f[0] for f in _lib.InstanceStatus._fields_]
-    body = "".join('printf("%%zu ", offsetof(ebb_instance_status, %s));' % n for n in names)
-    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "ebb_gb300.h"\nint main(void){%s'
-                   'printf("%%zu\\n", sizeof(ebb_instance_status));return 0;}\n' % body)
-    exe = tmp_path / "layout"
+@pytest.mark.parametrize("cname,pyname", [("ebb_instance_status", "InstanceStatus"),
+                                           ("ebb_server_options", "ServerOptions"),
+                                           ("ebb_request_result", "RequestResult"),
+                                           ("ebb_server_stats", "ServerStats")])
+def test_struct_layout_matches_header(tmp_path, cname, pyname):
+    """Field offsets and size of a public struct as a C compiler lays it out from the
+    header vs the ctypes binding."""
     import subprocess
+    st = getattr(_lib, pyname)
+    names = [f[0] for f in st._fields_]
+    body = "".join('printf("%%zu ", offsetof(%s, %s));' % (cname, n) for n in names)
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "ebb_gb300.h"\nint main(void){%s'
+                   'printf("%%zu\\n", sizeof(%s));return 0;}\n' % (body, cname))
+    exe = tmp_path / "layout"
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
     got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
-    want = [getattr(_lib.InstanceStatus, n).offset for n in names] + [C.sizeof(_lib.InstanceStatus)]
+    want = [getattr(st, n).offset for n in names] + [C.sizeof(st)]
     assert got == want
 
 
