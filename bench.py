@@ -43,6 +43,17 @@ def wedge_config(cfl=0.4):
                        "initialConditions": [2.5, 0, 1, 1], "boudaryConditions": WEDGE_BCS})
 
 
+def max_over_ranks(x):
+    """Barrier, then the maximum of x over all ranks (one independent replica per GPU:
+    the whole job is as slow as its slowest replica)."""
+    import torch
+    import torch.distributed as dist
+    dist.barrier()
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -162,12 +173,7 @@ def measure(L, E, _lib, gen, mesh, precision, args, local, ws, want_e2e):
     elapsed = dev_ms.value / 1e3
     steps_done = n.value
     if ws > 1:
-        import torch
-        import torch.distributed as dist
-        dist.barrier()
-        t = torch.tensor([elapsed], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
+        elapsed = max_over_ranks(elapsed)
     state = sol.state
     value = ws * ncell * steps_done / elapsed
     e2e = None
