@@ -157,6 +157,8 @@ SIGNATURES = {
     "ebb_server_destroy": (None, [_vp]),
     "ebb_save_solution": (C.c_int, [_vp, _cp, C.c_double, C.c_double]),
     "ebb_load_solution": (C.c_int, [_vp, _cp]),
+    "ebb_load_solution_parts": (C.c_int, [_vp, C.c_int32, C.POINTER(_cp)]),
+    "ebb_reconstruct": (C.c_int, [_vp, _vp, _cp, _cp, C.c_double, C.c_double, _dp, C.POINTER(C.c_int64)]),
 }
 
 _lib = None

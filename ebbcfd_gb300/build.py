@@ -16,6 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libebbgb300.so")
 CLI = os.path.join(OUT, "ebb-solve")
+RECON = os.path.join(OUT, "ebb-reconstruct")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU = {
@@ -23,7 +24,7 @@ CU = {
     "k_split.cu": ["-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"],
     "flux_noalloc.cu": ["-fmad=false"],
 }
-CPP = ["solver.cpp", "arena.cpp", "server.cpp", "host_mesh.cpp", "host_config.cpp", "host_io.cpp"]
+CPP = ["solver.cpp", "arena.cpp", "server.cpp", "reconstruct.cpp", "host_mesh.cpp", "host_config.cpp", "host_io.cpp"]
 
 
 def _nvcc():
@@ -38,17 +39,17 @@ def _cuda_home(nvcc):
 
 
 def _sources():
-    srcs = [os.path.join(CSRC, f) for f in list(CU) + CPP + ["ebb_solve.cpp"]]
+    srcs = [os.path.join(CSRC, f) for f in list(CU) + CPP + ["ebb_solve.cpp", "ebb_reconstruct.cpp"]]
     hdr = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".hpp", ".cuh"))]
     hdr.append(os.path.join(os.path.dirname(HERE), "include", "ebb_gb300.h"))
     return srcs, hdr
 
 
 def up_to_date():
-    if not os.path.exists(LIB) or not os.path.exists(CLI):
+    if not all(os.path.exists(f) for f in (LIB, CLI, RECON)):
         return False
     srcs, hdr = _sources()
-    t = min(os.path.getmtime(LIB), os.path.getmtime(CLI))
+    t = min(os.path.getmtime(f) for f in (LIB, CLI, RECON))
     return all(os.path.getmtime(f) <= t for f in srcs + hdr + [os.path.abspath(__file__)])
 
 
@@ -88,14 +89,16 @@ def build(force=False, verbose=False):
     if p.returncode != 0:
         raise RuntimeError("link failed: %s\n%s" % (" ".join(cmd), p.stdout))
     os.replace(tmp, LIB)
-    # the ebb-solve command-line driver, linked against the library (rpath $ORIGIN)
-    tmp = CLI + ".tmp%d" % os.getpid()
-    cmd = ["g++", "-O2", "-std=c++17", "-o", tmp, os.path.join(CSRC, "ebb_solve.cpp"), "-L" + OUT, "-lebbgb300",
-           "-Wl,-rpath,$ORIGIN"]
-    p = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
-    if p.returncode != 0:
-        raise RuntimeError("ebb-solve link failed: %s\n%s" % (" ".join(cmd), p.stdout))
-    os.replace(tmp, CLI)
+    # the ebb-solve and ebb-reconstruct command-line drivers, linked against the library
+    # (rpath $ORIGIN)
+    for exe, src in ((CLI, "ebb_solve.cpp"), (RECON, "ebb_reconstruct.cpp")):
+        tmp = exe + ".tmp%d" % os.getpid()
+        cmd = ["g++", "-O2", "-std=c++17", "-o", tmp, os.path.join(CSRC, src), "-L" + OUT, "-lebbgb300",
+               "-Wl,-rpath,$ORIGIN"]
+        p = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        if p.returncode != 0:
+            raise RuntimeError("%s link failed: %s\n%s" % (os.path.basename(exe), " ".join(cmd), p.stdout))
+        os.replace(tmp, exe)
     if verbose:
         print("built", LIB)
     return LIB

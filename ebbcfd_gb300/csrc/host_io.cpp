@@ -51,6 +51,21 @@ struct BE {
     }
 };
 
+// append the CRC-32 (over the body and 4 zero bytes, see above) and write the file
+int finish_and_write(BE &w, const char *path)
+{
+    const size_t body = w.b.size();
+    w.b.resize(body + 4, 0);
+    uint32_t c = crc32(w.b.data(), w.b.size());
+    w.b.resize(body);
+    for (int k = 0; k < 4; k++) w.u8((uint8_t)(c >> (8 * k)));
+    FILE *fp = std::fopen(path, "wb");
+    if (!fp) return EBB_ERR_IO;
+    size_t n = std::fwrite(w.b.data(), 1, w.b.size(), fp);
+    std::fclose(fp);
+    return n == w.b.size() ? EBB_OK : EBB_ERR_IO;
+}
+
 struct RD {
     const uint8_t *p, *end;
     bool ok = true;
@@ -89,6 +104,76 @@ struct RD {
 
 }  // namespace
 
+namespace ebb {
+
+// Cells of one .esln file (v1: states in order; v2: global id, edge count, state, face
+// states) into q by global id (loadSolution, io.d:218-366, partitioned form).
+int read_esln_into(const char *path, std::vector<double> &q, std::vector<uint8_t> &seen, double &t, double &dt)
+{
+    if (!path) return EBB_ERR_ARG;
+    FILE *fp = std::fopen(path, "rb");
+    if (!fp) return EBB_ERR_IO;
+    std::vector<uint8_t> buf;
+    uint8_t tmp[1 << 16];
+    size_t n;
+    while ((n = std::fread(tmp, 1, sizeof tmp, fp)) > 0) buf.insert(buf.end(), tmp, tmp + n);
+    std::fclose(fp);
+    RD r{buf.data(), buf.data() + buf.size()};
+    if (r.u32() != 0xEA98E1F5u || !r.ok) return EBB_ERR_FORMAT;
+    const uint32_t ver = r.u32();
+    const uint32_t cells = r.u32();
+    t = r.f64();
+    dt = r.f64();
+    const uint64_t C = seen.size();
+    if (!r.ok) return EBB_ERR_FORMAT;
+    if (ver == 1) {
+        if (cells != C) return EBB_ERR_FORMAT;
+        for (uint64_t i = 0; i < C; i++) {
+            for (int k = 0; k < 4; k++) q[4 * i + k] = r.f64();
+            seen[i] = 1;
+        }
+    } else if (ver == 2) {
+        const uint32_t M = r.u32();
+        (void)r.u32();
+        if (M != 4) return EBB_ERR_FORMAT;
+        for (uint32_t c = 0; c < cells && r.ok; c++) {
+            const uint32_t id = r.u32();
+            const int ne = r.u8();
+            if (id >= C) return EBB_ERR_FORMAT;
+            for (int k = 0; k < 4; k++) q[4 * (size_t)id + k] = r.f64();
+            for (int j = 0; j < ne; j++)
+                for (int k = 0; k < 4; k++) (void)r.f64();  // face states are recomputed by the next residual
+            seen[id] = 1;
+        }
+    } else {
+        return EBB_ERR_FORMAT;
+    }
+    return r.ok ? EBB_OK : EBB_ERR_FORMAT;
+}
+
+// .esln v2 of points without edges (the refined mesh of ebb-reconstruct,
+// reconstruct.d:418-420): entry i = global id i, 0 edges, q[i].
+int write_esln_points(const char *path, int64_t n, const double *q, double t, double dt, uint32_t order)
+{
+    BE w;
+    w.b.reserve(40 + (size_t)n * 37);
+    w.u32(0xEA98E1F5u);
+    w.u32(2);
+    w.u32((uint32_t)n);
+    w.f64(t);
+    w.f64(dt);
+    w.u32(4);
+    w.u32(order);
+    for (int64_t i = 0; i < n; i++) {
+        w.u32((uint32_t)i);
+        w.u8(0);
+        for (int k = 0; k < 4; k++) w.f64(q[4 * i + k]);
+    }
+    return finish_and_write(w, path);
+}
+
+}  // namespace ebb
+
 extern "C" {
 
 int ebb_save_solution(ebb_solver *s, const char *path, double t, double dt)
@@ -117,53 +202,28 @@ int ebb_save_solution(ebb_solver *s, const char *path, double t, double dt)
         for (int j = 0; j < ne; j++, fo++)
             for (int k = 0; k < 4; k++) w.f64(f[4 * fo + k]);
     }
-    const size_t body = w.b.size();
-    w.b.resize(body + 4, 0);
-    uint32_t c = crc32(w.b.data(), w.b.size());
-    w.b.resize(body);
-    for (int k = 0; k < 4; k++) w.u8((uint8_t)(c >> (8 * k)));
-    FILE *fp = std::fopen(path, "wb");
-    if (!fp) return EBB_ERR_IO;
-    size_t n = std::fwrite(w.b.data(), 1, w.b.size(), fp);
-    std::fclose(fp);
-    return n == w.b.size() ? EBB_OK : EBB_ERR_IO;
+    return finish_and_write(w, path);
 }
 
-int ebb_load_solution(ebb_solver *s, const char *path)
+int ebb_load_solution(ebb_solver *s, const char *path) { return ebb_load_solution_parts(s, 1, &path); }
+
+int ebb_load_solution_parts(ebb_solver *s, int32_t n, const char *const *paths)
 {
-    if (!s || !path) return EBB_ERR_ARG;
-    FILE *fp = std::fopen(path, "rb");
-    if (!fp) return EBB_ERR_IO;
-    std::vector<uint8_t> buf;
-    uint8_t tmp[1 << 16];
-    size_t n;
-    while ((n = std::fread(tmp, 1, sizeof tmp, fp)) > 0) buf.insert(buf.end(), tmp, tmp + n);
-    std::fclose(fp);
-    RD r{buf.data(), buf.data() + buf.size()};
-    if (r.u32() != 0xEA98E1F5u || !r.ok) return EBB_ERR_FORMAT;
-    uint32_t ver = r.u32();
-    uint32_t cells = r.u32();
-    if (!r.ok || cells != (uint32_t)s->C) return EBB_ERR_FORMAT;
-    double t = r.f64(), dt = r.f64();
+    if (!s || n <= 0 || !paths) return EBB_ERR_ARG;
     std::vector<double> q(4 * s->C);
-    if (ver == 1) {
-        for (int64_t i = 0; i < s->C; i++)
-            for (int k = 0; k < 4; k++) q[4 * i + k] = r.f64();
-    } else if (ver == 2) {
-        uint32_t M = r.u32();
-        (void)r.u32();
-        if (M != 4) return EBB_ERR_FORMAT;
-        for (int64_t i = 0; i < s->C; i++) {
-            (void)r.u32();
-            int ne = r.u8();
-            for (int k = 0; k < 4; k++) q[4 * i + k] = r.f64();
-            for (int j = 0; j < ne; j++)
-                for (int k = 0; k < 4; k++) (void)r.f64();  // face states are recomputed by the next residual
+    std::vector<uint8_t> seen(s->C, 0);
+    double t = 0, dt = 0;
+    for (int32_t k = 0; k < n; k++) {
+        double tk, dtk;
+        int r = ebb::read_esln_into(paths[k], q, seen, tk, dtk);
+        if (r) return r;
+        if (k == 0) {
+            t = tk;
+            dt = dtk;
         }
-    } else {
-        return EBB_ERR_FORMAT;
     }
-    if (!r.ok) return EBB_ERR_FORMAT;
+    for (int64_t i = 0; i < s->C; i++)
+        if (!seen[i]) return EBB_ERR_FORMAT;  // a cell no file covers
     int rc = ebb_set_state(s, q.data());
     if (rc) return rc;
     return ebb_set_time(s, t, dt);

@@ -417,6 +417,12 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? EBB_CELL_MINB_F : 1) k_c
             st4(gp + 4, nanv);
         }
     }
+    if (A.lim) {  // limiter values, exported for ebb-reconstruct
+        T *lp = reinterpret_cast<T *>(A.lim) + 8 * (size_t)i;
+        T a[4] = {lim0[0], lim1[0], lim0[1], lim1[1]}, b[4] = {lim0[2], lim1[2], lim0[3], lim1[3]};
+        st4(lp, a);
+        st4(lp + 4, b);
+    }
     T lg0[4], lg1[4];
     T l0 = T(1.0), l1 = T(1.0);
 #pragma unroll
@@ -1084,6 +1090,120 @@ int launch_update_impl(const DMesh &M, const DPhys &P, const DArrays &A, int sta
     return ret(cudaGetLastError());
 }
 
+// ---- ebb-reconstruct (app/reconstruct.d:239-424) --------------------------------
+// Edge values 0.5 (q[0] + q[1]) of every edge, at its reference edge id.  q[1] of a
+// boundary edge is what the boundary flux code of solve.d:769-968 leaves there:
+// the exact state at the midpoint (Dirichlet), the freestream (fullState), the ghost
+// state (inviscid wall, constant pressure, TP inflow), the face state with negated
+// momentum (viscous wall) or with reflected velocity (symmetry).
+template <typename T>
+__global__ void k_recon_edges(DMesh M, DArrays A, const T *__restrict__ qs, double *out)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= M.Eint + M.G) return;
+    const T *face = reinterpret_cast<const T *>(A.face);
+    T q0[4], q1[4];
+    int ref;
+    if (e < M.Eint) {
+        const int2 sl = reinterpret_cast<const int2 *>(M.e_slot)[e];
+        ld4(face + 4 * (size_t)sl.x, q0);
+        ld4(face + 4 * (size_t)sl.y, q1);
+        ref = M.e_ref[e];
+    } else {
+        const int b = e - M.Eint;
+        ld4(face + 4 * (size_t)M.b_slot[b], q0);
+        ref = M.b_ref[b];
+        const int type = M.b_type[b];
+        switch (type & 0xff) {
+        case BC_DIRICHLET:
+            ld4(ptr<T>(M.g.b_dmid) + 4 * (size_t)b, q1);
+            break;
+        case BC_FULLSTATE:
+            ld4(ptr<T>(M.g.b_data) + 4 * (size_t)b, q1);
+            break;
+        case BC_VISCWALL:
+            q1[0] = q0[0];
+            q1[1] = -q0[1];
+            q1[2] = -q0[2];
+            q1[3] = q0[3];
+            break;
+        case BC_SYMMETRY: {
+            T v0 = q0[1] / q0[0], v1 = q0[2] / q0[0], n0, n1;
+            reflect(type, ptr<T>(M.g.b_refl) + 4 * (size_t)b, v0, v1, n0, n1);
+            q1[0] = q0[0];
+            q1[1] = q0[0] * n0;
+            q1[2] = q0[0] * n1;
+            q1[3] = q0[3];
+            break;
+        }
+        default:  // inviscid wall, constant pressure, TP inflow: the ghost state
+            ld4(qs + 4 * ((size_t)M.C + b), q1);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) out[4 * (size_t)ref + k] = 0.5 * ((double)q0[k] + (double)q1[k]);
+}
+
+// Node values of the nodes the elements use.  Interior node: the average over the
+// node's cells (reference element order) of q + lim0 g0 dx + lim1 g1 dy at the node
+// (reconstruct.d:303-324); boundary node: the average of the edge values of the
+// boundary edges its cells share with it (reconstruct.d:326-346).  A NaN value records
+// the lowest node index in *err (reconstruct.d enforces no NaN).
+template <typename T>
+__global__ void k_recon_nodes(DMesh M, DArrays A, int n, const int32_t *__restrict__ off,
+                              const int32_t *__restrict__ items, const uint8_t *__restrict__ is_b,
+                              const double *__restrict__ nxy, const double *__restrict__ cxy,
+                              const double *__restrict__ edge_vals, double *out, unsigned long long *err)
+{
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    double s[4] = {0.0, 0.0, 0.0, 0.0};
+    const int a0 = off[v], a1 = off[v + 1];
+    if (!is_b[v]) {
+        const T *g = reinterpret_cast<const T *>(A.grad);
+        const T *l = reinterpret_cast<const T *>(A.lim);
+        for (int a = a0; a < a1; a++) {
+            const int c = items[a];  // device cell
+            const double dx = nxy[2 * (size_t)v] - cxy[2 * (size_t)c];
+            const double dy = nxy[2 * (size_t)v + 1] - cxy[2 * (size_t)c + 1];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const double q = A.q64[4 * (size_t)c + k];
+                const double g0 = (double)g[8 * (size_t)c + 2 * k], g1 = (double)g[8 * (size_t)c + 2 * k + 1];
+                const double l0 = (double)l[8 * (size_t)c + 2 * k], l1 = (double)l[8 * (size_t)c + 2 * k + 1];
+                s[k] += q + l0 * g0 * dx + l1 * g1 * dy;
+            }
+        }
+    } else {
+        for (int a = a0; a < a1; a++) {
+            const int e = items[a];  // reference edge id
+#pragma unroll
+            for (int k = 0; k < 4; k++) s[k] += edge_vals[4 * (size_t)e + k];
+        }
+    }
+    const double r = 1.0 / (double)(a1 - a0);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        s[k] *= r;
+        out[4 * (size_t)v + k] = s[k];
+    }
+    if (isnan(s[0]) || isnan(s[1]) || isnan(s[2]) || isnan(s[3])) atomicMin(err, (unsigned long long)v);
+}
+
+template <typename T>
+int launch_recon_impl(const DMesh &M, const DArrays &A, const T *qs, double *edge_out, int n_nodes,
+                      const int32_t *off, const int32_t *items, const uint8_t *is_b, const double *nxy,
+                      const double *cxy, double *node_out, unsigned long long *err, void *stream)
+{
+    cudaStream_t st = (cudaStream_t)stream;
+    const int ne = M.Eint + M.G;
+    if (ne > 0) k_recon_edges<T><<<(ne + 255) / 256, 256, 0, st>>>(M, A, qs, edge_out);
+    if (n_nodes > 0)
+        k_recon_nodes<T><<<(n_nodes + 255) / 256, 256, 0, st>>>(M, A, n_nodes, off, items, is_b, nxy, cxy, edge_out,
+                                                                node_out, err);
+    return ret(cudaGetLastError());
+}
+
 }  // namespace ebbdev
 
 #define EBB_INSTANTIATE(T)                                                                                        \
@@ -1102,4 +1222,12 @@ int launch_update_impl(const DMesh &M, const DPhys &P, const DArrays &A, int sta
                          int dt_update, int need_dt, int final_stage, void *stream)                               \
     {                                                                                                             \
         return ebbdev::launch_update_impl<T>(M, P, A, stage, qin, qout, dt_update, need_dt, final_stage, stream); \
+    }                                                                                                             \
+    template <>                                                                                                   \
+    int launch_recon<T>(const DMesh &M, const DArrays &A, const T *qs, double *edge_out, int n_nodes,            \
+                        const int32_t *off, const int32_t *items, const uint8_t *is_b, const double *nxy,         \
+                        const double *cxy, double *node_out, unsigned long long *err, void *stream)               \
+    {                                                                                                             \
+        return ebbdev::launch_recon_impl<T>(M, A, qs, edge_out, n_nodes, off, items, is_b, nxy, cxy, node_out,   \
+                                            err, stream);                                                         \
     }

@@ -104,6 +104,7 @@ struct DArrays {
     void *qs;             // later-stage input in T
     void *aux;            // k1 / R1 / RK4 accumulator in T
     void *face, *grad, *fl, *fs, *cdt, *R;
+    void *lim;            // T[8] per cell (lim[k][0], lim[k][1]) when exported, else null
     double *red;          // per-block partial sums (8 per block)
     DState *st;
     DRecord *rec;
@@ -129,6 +130,19 @@ template <>
 int launch_update<float>(const DMesh &, const DPhys &, const DArrays &, int, const float *, float *, int, int, int,
                          void *);
 int launch_step_end(const DMesh &M, const DArrays &A, int nred_blocks, int split, void *stream);
+// ebb-reconstruct: edge values (reference edge order) and node values
+template <typename T>
+int launch_recon(const DMesh &M, const DArrays &A, const T *qs, double *edge_out, int n_nodes, const int32_t *off,
+                 const int32_t *items, const uint8_t *is_b, const double *nxy, const double *cxy, double *node_out,
+                 unsigned long long *err, void *stream);
+template <>
+int launch_recon<double>(const DMesh &, const DArrays &, const double *, double *, int, const int32_t *,
+                         const int32_t *, const uint8_t *, const double *, const double *, double *,
+                         unsigned long long *, void *);
+template <>
+int launch_recon<float>(const DMesh &, const DArrays &, const float *, double *, int, const int32_t *,
+                        const int32_t *, const uint8_t *, const double *, const double *, double *,
+                        unsigned long long *, void *);
 int update_grid(const DMesh &M);
 int launch_flux_batch(int kind, int64_t n, const double *qL, const double *qR, const double *nrm, double *F,
                       double *s, void *stream);

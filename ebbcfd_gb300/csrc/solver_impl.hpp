@@ -70,4 +70,6 @@ int solver_run_residual_on_qs(ebb_solver *s, int limit, int dt_update, double *n
 int build_instance(const ebb_mesh *mesh, const ebb_config *cfg, InstLayout &L, std::string &err);
 int assemble(ebb_solver *s, std::vector<InstLayout> &layouts, int32_t precision, std::string &err);
 size_t arena_bytes(const std::vector<InstLayout> &layouts, int32_t precision);
+int read_esln_into(const char *path, std::vector<double> &q, std::vector<uint8_t> &seen, double &t, double &dt);
+int write_esln_points(const char *path, int64_t n, const double *q, double t, double dt, uint32_t order);
 }  // namespace ebb

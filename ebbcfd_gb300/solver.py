@@ -270,6 +270,28 @@ class UfvmSolver:
     def load_solution(self, path):
         self._raise(_lib.load().ebb_load_solution(self.h, str(path).encode()))
 
+    def load_solution_parts(self, paths):
+        """loadSolution of every rank's file of a partitioned run (cells by global id)."""
+        arr = (C.c_char_p * len(paths))(*[str(p).encode() for p in paths])
+        self._raise(_lib.load().ebb_load_solution_parts(self.h, len(paths), arr))
+
+    def reconstruct(self, mmsh_path=None, esln_path=None, t=None, dt=None):
+        """ebb-reconstruct (app/reconstruct.d:79-424) of the resident state: returns the
+        (n, 4) values of the refined mesh (used nodes, edge midpoints, cells) and writes
+        the .mmsh / .esln files when paths are given."""
+        L = _lib.load()
+        n = C.c_int64()
+        self._raise(L.ebb_reconstruct(self.h, self.mesh.h, None, None, 0.0, 0.0, None, C.byref(n)))
+        if t is None or dt is None:
+            t0, dt0, _ = self.time()
+            t = t0 if t is None else t
+            dt = dt0 if dt is None else dt
+        q = np.zeros((n.value, 4))
+        self._raise(L.ebb_reconstruct(self.h, self.mesh.h, None if mmsh_path is None else str(mmsh_path).encode(),
+                                      None if esln_path is None else str(esln_path).encode(), float(t), float(dt),
+                                      _dp(q), C.byref(n)))
+        return q
+
     def status(self, first=0, count=None):
         """list of dicts (cell_offset, n_cells, iterations, t, dt, cfl, done, status, err_index,
         drag, lift, resid, rmax, resid_first) for instances first..first+count-1"""

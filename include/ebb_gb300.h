@@ -18,6 +18,7 @@
  *   ebb_flux               source/flux.d:66-141,224-303  rusanovFlux!4 / roeFlux!4 (qL, qR, n, ref sMax)
  *   ebb_save_solution      source/io.d:68-161        saveSolution (.esln v2, big-endian)
  *   ebb_load_solution      source/io.d:218-366       loadSolution
+ *   ebb_reconstruct        app/reconstruct.d:79-424  ebb-reconstruct (refined .mmsh / .esln)
  */
 #ifndef EBB_GB300_H
 #define EBB_GB300_H
@@ -357,6 +358,26 @@ int ebb_flux_noalloc(int32_t kind, int64_t n, const double *qL, const double *qR
    takes them as arguments: the driver saves before advancing t). */
 int ebb_save_solution(ebb_solver *s, const char *path, double t, double dt);
 int ebb_load_solution(ebb_solver *s, const char *path);
+/* loadSolution of a partitioned run (io.d:218-366): every file's cells go to their
+   global ids; t and dt come from the first file; EBB_ERR_FORMAT unless every cell is
+   covered. */
+int ebb_load_solution_parts(ebb_solver *s, int32_t n, const char *const *paths);
+
+/* ---- ebb-reconstruct (app/reconstruct.d:79-424) ---------------------------
+   One residual evaluation of the resident state (limited as the config's "limited",
+   no time-step update) gives gradients, limiters and the states on both sides of
+   every edge; the refined mesh then has, as points: the nodes the elements use (node
+   order), the edge midpoints (reference edge order) and the cell centroids, each
+   cell split into 2 x nEdges triangles; its values: node values (the average over
+   the node's cells of the limited gradient extrapolation to the node; boundary nodes
+   average the values of their boundary edges), edge values (mean of the edge's two
+   states) and the cell averages.  mmsh_path / esln_path (may be NULL) receive the
+   .mmsh and .esln files of the refined mesh (t, dt in the .esln header); q_out (may
+   be NULL) receives the n_out x 4 values; with all three NULL only *n_out is set.
+   The mesh is the one the solver was created from.  EBB_ERR_NAN_CELL (index = node)
+   when a node value is NaN, as the reference refuses. */
+int ebb_reconstruct(ebb_solver *s, const ebb_mesh *mesh, const char *mmsh_path, const char *esln_path, double t,
+                    double dt, double *q_out, int64_t *n_out);
 
 #ifdef __cplusplus
 }

@@ -1754,6 +1754,95 @@ void o_grad_lim(const OMesh *m, double *grad, double *lim)
         }
 }
 
+/* ebb-reconstruct (app/reconstruct.d:79-424): one ufvmSolver evaluation of the current
+   state limited as config.limited, without dt update (reconstruct.d:165-176), then the
+   refined triangulation's values: node values for the nodes the elements use, in node
+   order (interior nodes: the average over the node's elements, in element order, of
+   q + lim0*g0*dx + lim1*g1*dy at the node, reconstruct.d:303-324; boundary nodes: the
+   average of the values of the boundary edges of those elements that touch the node,
+   reconstruct.d:326-346), edge values 0.5*(q[0] + q[1]) in edge order
+   (reconstruct.d:290-294), and the cell averages.  out holds (n_nodes_used + nEdges +
+   nInterior) x 4 values; sizes[0..2] receive the three counts.  Returns 0, or an error
+   status (NaN flux; NaN node value: O_ERR_NAN_CELL with the node index). */
+int o_reconstruct(OMesh *m, double *out, int *sizes)
+{
+    const int C = m->nInterior;
+    double newDt = INFINITY, Rmax = 0.0;
+    int st = o_solver(m, m->R, m->q, &newDt, &Rmax, m->cfg.limited, 0);
+    if (st) return st;
+    /* node -> elements (ascending), used nodes, boundary nodes */
+    int *cnt = calloc((size_t)m->nNodes + 1, sizeof(int));
+    for (int c = 0; c < m->nElem; c++)
+        for (int k = m->elemOff[c]; k < m->elemOff[c + 1]; k++) cnt[m->elemNodes[k] - 1 + 1]++;
+    for (int n = 0; n < m->nNodes; n++) cnt[n + 1] += cnt[n];
+    int *fill = calloc((size_t)m->nNodes, sizeof(int));
+    int *ncell = malloc(sizeof(int) * (size_t)(cnt[m->nNodes] > 0 ? cnt[m->nNodes] : 1));
+    for (int c = 0; c < m->nElem; c++)
+        for (int k = m->elemOff[c]; k < m->elemOff[c + 1]; k++) {
+            int n = m->elemNodes[k] - 1;
+            ncell[cnt[n] + fill[n]++] = c;
+        }
+    char *isB = calloc((size_t)m->nNodes, 1);
+    for (int b = 0; b < m->nB; b++) {
+        isB[m->bNodes[b][0]] = 1;
+        isB[m->bNodes[b][1]] = 1;
+    }
+    double (*ev)[4] = malloc(sizeof(double[4]) * (size_t)(m->nEdges > 0 ? m->nEdges : 1));
+    for (int e = 0; e < m->nEdges; e++)
+        for (int k = 0; k < 4; k++) ev[e][k] = 0.5 * (m->edges[e].q[0][k] + m->edges[e].q[1][k]);
+    int nUsed = 0, status = 0;
+    for (int n = 0; n < m->nNodes && !status; n++) {
+        int nc = cnt[n + 1] - cnt[n];
+        if (nc == 0) continue; /* orphaned node (reconstruct.d:247-268) */
+        double v[4] = {0, 0, 0, 0};
+        if (!isB[n]) {
+            for (int a = cnt[n]; a < cnt[n + 1]; a++) {
+                const OCell *c = &m->cells[ncell[a]];
+                double dx = m->nodes[n][0] - c->centroid[0];
+                double dy = m->nodes[n][1] - c->centroid[1];
+                for (int k = 0; k < 4; k++)
+                    v[k] += m->q[ncell[a]][k] + c->lim[k][0] * c->grad[k][0] * dx + c->lim[k][1] * c->grad[k][1] * dy;
+            }
+            for (int k = 0; k < 4; k++) v[k] *= (1.0 / nc);
+        } else {
+            int ne = 0;
+            for (int a = cnt[n]; a < cnt[n + 1]; a++) {
+                int ci = ncell[a];
+                const OCell *c = &m->cells[ci];
+                for (uint32_t j = 0; j < c->nEdges; j++) {
+                    int n1 = m->elemNodes[m->elemOff[ci] + (int)j] - 1;
+                    int n2 = m->elemNodes[m->elemOff[ci] + (int)((j + 1) % c->nEdges)] - 1;
+                    const OEdge *e = &m->edges[c->edges[j]];
+                    if (e->isBoundary && (n1 == n || n2 == n)) {
+                        for (int k = 0; k < 4; k++) v[k] += ev[c->edges[j]][k];
+                        ne++;
+                    }
+                }
+            }
+            for (int k = 0; k < 4; k++) v[k] *= (1.0 / ne);
+        }
+        if (isnan(v[0]) || isnan(v[1]) || isnan(v[2]) || isnan(v[3])) {
+            m->errIndex = n;
+            status = O_ERR_NAN_CELL;
+        }
+        for (int k = 0; k < 4; k++) out[4 * nUsed + k] = v[k];
+        nUsed++;
+    }
+    if (!status) {
+        memcpy(out + 4 * (size_t)nUsed, ev, sizeof(double[4]) * (size_t)m->nEdges);
+        memcpy(out + 4 * ((size_t)nUsed + m->nEdges), m->q, sizeof(double[4]) * (size_t)C);
+        sizes[0] = nUsed;
+        sizes[1] = m->nEdges;
+        sizes[2] = C;
+    }
+    free(cnt);
+    free(fill);
+    free(ncell);
+    free(isB);
+    free(ev);
+    return status;
+}
+
 /* Thread count of the parallel loops (default 1).  Per-cell and per-edge work is
    independent, min/max reductions are exact, and errors report the first index in
    loop order, so results do not depend on it except for the last bits of the RMS

@@ -91,6 +91,8 @@ def lib():
         L.o_ms_converge.restype = C.c_long
         L.o_face_states.argtypes = [C.c_void_p, dp]
         L.o_grad_lim.argtypes = [C.c_void_p, dp, dp]
+        L.o_reconstruct.argtypes = [C.c_void_p, dp, ip]
+        L.o_reconstruct.restype = C.c_int
         L.o_flux_batch.argtypes = [C.c_int, C.c_int, dp, dp, dp, dp, dp]
         L.o_diffusive_flux.argtypes = [C.c_double, C.c_double, dp, dp, dp, dp]
         L.o_mms_eval.argtypes = [C.c_int, C.c_int, dp, dp, dp, dp, C.POINTER(OCfg)]
@@ -244,6 +246,18 @@ class OracleMesh:
         l = np.zeros((self.n_cells, 4, 2))
         lib().o_grad_lim(self.h, _dp(g), _dp(l))
         return g, l
+
+    def reconstruct(self):
+        """ebb-reconstruct values (reconstruct.d:79-424): (node values, edge values, cell
+        averages) as three (n, 4) arrays."""
+        n_nodes = len(self.mesh["nodes"])
+        out = np.zeros((n_nodes + self.n_edges + self.n_cells, 4))
+        cnt = np.zeros(3, dtype=np.int32)
+        st = lib().o_reconstruct(self.h, _dp(out), _ip(cnt))
+        if st:
+            raise RuntimeError("oracle reconstruct failed with status %d at index %d" % (st, lib().o_err_index(self.h)))
+        a, b, c = (int(x) for x in cnt)
+        return out[:a].copy(), out[a:a + b].copy(), out[a + b:a + b + c].copy()
 
     def ms_converge(self, max_iter, tol=1e-10):
         l2 = np.zeros(4)
