@@ -1,7 +1,7 @@
 // arena.cpp -- device layout of one or many meshes (buildMesh + ufvmSetup per instance,
 // source/mesh.d:217-643 and source/solve.d:175-279), assembled into one arena.
 //
-// Each instance is laid out on its own first (RCM cell order, ghosts by owner, interior
+// Each instance is laid out on its own first (Hilbert cell order, ghosts by owner, interior
 // edges by first cell, FP64 geometry), in local numbering.  The arena concatenates the
 // instances: interior cells of every instance first, then every instance's ghost
 // cells, interior edges first then boundary edges, face slots in one ELL array whose
@@ -88,7 +88,7 @@ int build_instance(const ebb_mesh *mesh, const ebb_config *cfg, InstLayout &L, s
     L.mu = cfg->viscosity ? (cfg->ic[3] * 1.0 * cfg->l_ref) / cfg->re : NAN;
 
     // ---- orderings ----------------------------------------------------------
-    L.perm = rcm_order(t);
+    L.perm = hilbert_order(t);
     std::vector<int32_t> inv(C);
     for (int64_t k = 0; k < C; k++) inv[L.perm[k]] = (int32_t)k;
     std::vector<int32_t> gorder(G);  // local ghost b -> reference ghost

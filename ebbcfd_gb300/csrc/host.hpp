@@ -2,7 +2,7 @@
 //
 // The host keeps the reference's mesh semantics (gmsh reader of source/io.d:689-990,
 // buildMesh of source/mesh.d:217-643) and turns them into the device layout:
-// RCM-renumbered cells, ELL ("slot-major") per-face arrays, edge lists sorted by
+// Hilbert-ordered cells, ELL ("slot-major") per-face arrays, edge lists sorted by
 // their first cell, all precomputed in FP64.
 #pragma once
 
@@ -55,8 +55,8 @@ struct Topology {
 
 bool build_topology(const ebb_mesh &m, Topology &t, std::string &err);
 
-// Reverse Cuthill-McKee order of the interior cells: perm[new] = old.
-std::vector<int32_t> rcm_order(const Topology &t);
+// Hilbert-curve order of the cell centroids: perm[new] = old.
+std::vector<int32_t> hilbert_order(const Topology &t);
 
 // JSON
 bool parse_config_json(const char *text, ebb_config *out, std::string &err);

@@ -1,4 +1,4 @@
-// host_mesh.cpp -- gmsh 2.2 reader, topology/geometry build and RCM ordering.
+// host_mesh.cpp -- gmsh 2.2 reader, topology/geometry build and the cell ordering.
 //
 // Reader semantics follow source/io.d:689-990 (parseGmshMesh); topology and FP64
 // geometry follow source/mesh.d:217-381,481-642 (UMesh2.buildMesh).  The design is
@@ -583,71 +583,45 @@ bool build_topology(const ebb_mesh &m, Topology &t, std::string &err)
     return true;
 }
 
-std::vector<int32_t> rcm_order(const Topology &t)
+// Hilbert-curve order of the cell centroids (the curve's index of each centroid on a
+// 2^16 x 2^16 grid over the bounding box, by the classic bit-by-bit quadrant
+// rotation): consecutive cells form compact patches of the plane, so the cells a
+// thread block handles are mostly each other's neighbours.
+std::vector<int32_t> hilbert_order(const Topology &t)
 {
     const int64_t C = t.C;
-    const int K = kMaxEdges;
-    std::vector<int32_t> deg(C, 0);
-    for (int64_t i = 0; i < C; i++)
-        for (int j = 0; j < t.nedge[i]; j++)
-            if (t.slot_nbr[i * K + j] < C) deg[i]++;
-    std::vector<int32_t> order;
-    order.reserve(C);
-    std::vector<int32_t> level(C, -1);
-    std::vector<char> done(C, 0);
-    std::vector<int32_t> q;
-    q.reserve(C);
-    // BFS returning the last vertex of lowest degree in the deepest level
-    auto bfs_far = [&](int32_t s) {
-        std::vector<int32_t> seen;
-        q.clear();
-        q.push_back(s);
-        level[s] = 0;
-        seen.push_back(s);
-        for (size_t h = 0; h < q.size(); h++) {
-            int32_t v = q[h];
-            for (int j = 0; j < t.nedge[v]; j++) {
-                int32_t w = t.slot_nbr[(int64_t)v * K + j];
-                if (w < C && level[w] < 0) {
-                    level[w] = level[v] + 1;
-                    q.push_back(w);
-                    seen.push_back(w);
-                }
-            }
-        }
-        int32_t far = q.back();
-        int32_t best = far;
-        for (int32_t v : q)
-            if (level[v] == level[far] && deg[v] < deg[best]) best = v;
-        for (int32_t v : seen) level[v] = -1;
-        return best;
-    };
-    std::vector<int32_t> byDeg(C);
-    std::iota(byDeg.begin(), byDeg.end(), 0);
-    std::stable_sort(byDeg.begin(), byDeg.end(), [&](int32_t a, int32_t b) { return deg[a] < deg[b]; });
-    std::vector<int32_t> nb;
-    for (int32_t s0 : byDeg) {
-        if (done[s0]) continue;
-        int32_t s = bfs_far(bfs_far(s0));
-        if (done[s]) s = s0;
-        size_t head = order.size();
-        order.push_back(s);
-        done[s] = 1;
-        for (size_t h = head; h < order.size(); h++) {
-            int32_t v = order[h];
-            nb.clear();
-            for (int j = 0; j < t.nedge[v]; j++) {
-                int32_t w = t.slot_nbr[(int64_t)v * K + j];
-                if (w < C && !done[w]) {
-                    done[w] = 1;
-                    nb.push_back(w);
-                }
-            }
-            std::sort(nb.begin(), nb.end(), [&](int32_t a, int32_t b) { return deg[a] < deg[b] || (deg[a] == deg[b] && a < b); });
-            order.insert(order.end(), nb.begin(), nb.end());
-        }
+    double x0 = INFINITY, x1 = -INFINITY, y0 = INFINITY, y1 = -INFINITY;
+    for (int64_t i = 0; i < C; i++) {
+        x0 = std::min(x0, t.cx[i]);
+        x1 = std::max(x1, t.cx[i]);
+        y0 = std::min(y0, t.cy[i]);
+        y1 = std::max(y1, t.cy[i]);
     }
-    std::reverse(order.begin(), order.end());
+    const double span = std::max(std::max(x1 - x0, y1 - y0), 1e-300);
+    const uint32_t n = 1u << 16;
+    std::vector<uint64_t> key(C);
+    for (int64_t i = 0; i < C; i++) {
+        uint32_t x = (uint32_t)std::min<double>(n - 1, std::floor((t.cx[i] - x0) / span * (n - 1)));
+        uint32_t y = (uint32_t)std::min<double>(n - 1, std::floor((t.cy[i] - y0) / span * (n - 1)));
+        uint64_t d = 0;
+        for (uint32_t sq = n / 2; sq > 0; sq /= 2) {
+            const uint32_t rx = (x & sq) ? 1 : 0, ry = (y & sq) ? 1 : 0;
+            d += (uint64_t)sq * sq * ((3 * rx) ^ ry);
+            if (ry == 0) {  // rotate the quadrant
+                if (rx == 1) {
+                    x = sq - 1 - (x & (sq - 1));
+                    y = sq - 1 - (y & (sq - 1));
+                }
+                std::swap(x, y);
+            }
+            x &= sq - 1;
+            y &= sq - 1;
+        }
+        key[i] = d;
+    }
+    std::vector<int32_t> order(C);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return key[a] < key[b]; });
     return order;
 }
 

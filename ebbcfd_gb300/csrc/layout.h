@@ -1,6 +1,6 @@
 // layout.h -- device-resident mesh and solver state, shared by host and kernels.
 //
-// HBM layout (C interior cells in RCM order, G ghost cells = boundary edges ordered by
+// HBM layout (C interior cells in Hilbert-curve order, G ghost cells = boundary edges ordered by
 // owner, Eint interior edges sorted by first cell, Cs = C rounded up to 32):
 //   state   q64 double[4] per cell (32 B, one sector) = the solution; stage inputs qs1/qs
 //           in the arithmetic type T (double: qs1 aliases q64; float: a float[4] shadow),
