@@ -723,7 +723,6 @@ __global__ void __launch_bounds__(UPD_THREADS, sizeof(T) == 4 ? EBB_UPD_MINB_F :
     }
     DState *st = A.st + inst;
     if (halted(st)) return;
-    __shared__ double sh[UPD_THREADS / 32][10];
     const bool act = i < iend;
     double dtc = INFINITY, rm = 0.0;
     double ss[4] = {0, 0, 0, 0}, vs[4] = {0, 0, 0, 0};
@@ -990,39 +989,54 @@ __global__ void __launch_bounds__(UPD_THREADS, sizeof(T) == 4 ? EBB_UPD_MINB_F :
                 for (int k = 0; k < 8; k++) A.red[8 * (size_t)blockIdx.x + k] = (double)s8[k];
         }
         return;
-    } else {
-        dtc = warp_min(dtc);
-        rm = warp_max(rm);
+    } else if constexpr (!SPLIT) {
+        // FP64: every thread's values go to shared memory, and whole warps reduce
+        // columns, one lane per (column, group of 16 rows): an FP64 warp instruction
+        // costs the same with 1 or 32 lanes active, so a shuffle tree per value (5
+        // levels x 10 values per warp) would spend most of the kernel's FP64 time here.
+        // Column 1 holds -Rmax so that every column of warp 0 is a min.  Fixed order.
+        constexpr int W = 11;  // row stride in doubles: conflict-free strided reads
+        __shared__ double shr[UPD_THREADS * W];
+        __shared__ double part[10][16];
+        const int t = threadIdx.x;
+        const int ncol = final_stage ? 10 : 2;
+        shr[t * W + 0] = dtc;
+        shr[t * W + 1] = -rm;
         if (final_stage) {
 #pragma unroll
             for (int k = 0; k < 4; k++) {
-                ss[k] = warp_sum(ss[k]);
-                vs[k] = warp_sum(vs[k]);
+                shr[t * W + 2 + k] = ss[k];
+                shr[t * W + 6 + k] = vs[k];
             }
         }
-    }
-    if (lane == 0) {
-        sh[w][0] = dtc;
-        sh[w][1] = rm;
-        for (int k = 0; k < 4; k++) {
-            sh[w][2 + k] = ss[k];
-            sh[w][6 + k] = vs[k];
+        __syncthreads();
+        if (t < 16 * ncol) {  // group g of column c: rows g, g+16, ..., g+240
+            const int c = t >> 4, g = t & 15;
+            double a = shr[g * W + c];
+            if (c < 2) {
+                for (int r = 1; r < UPD_THREADS / 16; r++) a = fmin(a, shr[(g + 16 * r) * W + c]);
+            } else {
+                for (int r = 1; r < UPD_THREADS / 16; r++) a = a + shr[(g + 16 * r) * W + c];
+            }
+            part[c][g] = a;
         }
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double a = sh[0][0], b = sh[0][1];
-        double s8[8];
-        for (int k = 0; k < 8; k++) s8[k] = sh[0][2 + k];
-        for (int ww = 1; ww < UPD_THREADS / 32; ww++) {
-            a = fmin(a, sh[ww][0]);
-            b = fmax(b, sh[ww][1]);
-            for (int k = 0; k < 8; k++) s8[k] = s8[k] + sh[ww][2 + k];
+        __syncthreads();
+        if (t < ncol) {
+            double a = part[t][0];
+            if (t < 2) {
+                for (int g = 1; g < 16; g++) a = fmin(a, part[t][g]);
+            } else {
+                for (int g = 1; g < 16; g++) a = a + part[t][g];
+            }
+            if (t == 0) {
+                if (need_dt && a == a) atomicMin(&st->newdt_bits, (unsigned long long)__double_as_longlong(a));
+            } else if (t == 1) {
+                const double b = -a;
+                if (b > 0) atomicMax(&st->rmax_bits, (unsigned long long)__double_as_longlong(b));
+            } else {
+                A.red[8 * (size_t)blockIdx.x + (t - 2)] = a;
+            }
         }
-        if (need_dt && a == a) atomicMin(&st->newdt_bits, (unsigned long long)__double_as_longlong(a));
-        if (b > 0) atomicMax(&st->rmax_bits, (unsigned long long)__double_as_longlong(b));
-        if (final_stage)
-            for (int k = 0; k < 8; k++) A.red[8 * (size_t)blockIdx.x + k] = s8[k];
     }
 }
 
