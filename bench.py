@@ -228,13 +228,13 @@ def run_ours(args, ws, rank, local):
     m64 = measure(L, E, _lib, gen, mesh, "fp64", args, local, ws, not args.no_e2e)
     split = None
     if not args.no_split:
-        m32 = measure(L, E, _lib, gen, mesh, "split", args, local, ws, False)
+        m32 = measure(L, E, _lib, gen, mesh, "split", args, local, ws, not args.no_e2e)
         q64, q32 = m64["state"], m32["state"]
         scale = np.maximum(np.abs(q64).max(axis=0), 1e-300)
         split = {"value": m32["value"], "unit": "cell-updates/s", "ms_per_step": 1e3 * m32["elapsed"] / m32["steps"],
                  "speedup_vs_fp64": m32["value"] / m64["value"], "roofline": m32["roofline"],
                  "state_rel_err_vs_fp64": float((np.abs(q32 - q64).max(axis=0) / scale).max()),
-                 "steps_compared": m64["steps"] + args.warmup, "clocks": m32["clocks"]}
+                 "steps_compared": m64["steps"] + args.warmup, "clocks": m32["clocks"], "e2e": m32["e2e"]}
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(gen, ncell, budget_s=args.cpu_budget)
