@@ -363,21 +363,21 @@ def run_plate(args):
     return out
 
 
-def bump_json(mach, cfl=0.3):
+def bump_json(mach, cfl=0.3, integrator="RK2_TVD"):
     q = [mach, 0, 1, 1]
     return json.dumps({"mesh": "bump.msh", "dt": 1e-4, "tEnd": 1e9, "flux": "roeFlux", "saveIter": -1,
-                       "plotIter": -1, "forceBoundary": "Wall", "integrator": "RK2_TVD", "limited": True, "CFL": cfl,
+                       "plotIter": -1, "forceBoundary": "Wall", "integrator": integrator, "limited": True, "CFL": cfl,
                        "initialConditions": q,
                        "boudaryConditions": [{"tag": "Inflow", "type": "fullState", "q": q},
                                              {"tag": "Outflow", "type": "fullState", "q": q},
                                              {"tag": "Wall", "type": "inviscidWall", "q": q}]})
 
 
-def cylinder_json(re, mach=0.2, cfl=0.3):
+def cylinder_json(re, mach=0.2, cfl=0.3, integrator="RK2_TVD"):
     q = [mach, 0, 1, 1]
     far = [{"tag": t, "type": "fullState", "q": q} for t in ("Inflow", "Outflow", "Top", "Bottom")]
     return json.dumps({"mesh": "cyl.msh", "dt": 1e-4, "tEnd": 1e9, "flux": "roeFlux", "saveIter": -1,
-                       "plotIter": -1, "forceBoundary": "Cylinder", "integrator": "RK2_TVD", "limited": True,
+                       "plotIter": -1, "forceBoundary": "Cylinder", "integrator": integrator, "limited": True,
                        "CFL": cfl, "viscosity": True, "initialConditions": q,
                        "physicalConfig": {"Pr": 0.72, "R": 1.0, "gamma": 1.4, "Re": re, "L": 1.0},
                        "boudaryConditions": far + [{"tag": "Cylinder", "type": "viscidWall", "q": q}]})
@@ -505,7 +505,11 @@ def run_serve(args):
     gens = gen_meshes([(str(k), int(c), float(h), i) for i, (k, c, h) in enumerate(zip(kinds, cells, hs))])
     meshes = [g.to_solver_mesh() for g in gens]
     mesh_s = time.time() - t0
-    cfgs = [E.load_config(bump_json(float(m)) if k == "bump" else cylinder_json(float(r)))
+    # the served stream names no integrator: RK2 with multistage limiting, which stays
+    # bounded where the reference's TVD-RK2 (second stage always unlimited) lets FP32
+    # rounding grow into a NaN on some meshes
+    cfgs = [E.load_config(bump_json(float(m), integrator=args.serve_integrator) if k == "bump"
+                          else cylinder_json(float(r), integrator=args.serve_integrator))
             for k, m, r in zip(kinds, machs, res)]
     L = _lib.load()
     sv = E.EbbServer("split", hbm_budget=int(150e9), build_threads=8)
@@ -539,12 +543,15 @@ def run_serve(args):
     # sequential plain FP64: per-step device time alone x steps run
     per = seq_ms_per_step(L, E, meshes, cfgs, "fp64", args.seq_steps, 3)
     seq_s = float(sum(per[k] * iters[k] for k in range(R)) / 1e3)
-    return {"workload": "served-bump70-cyl30-split", "requests": R, "arrival_rate_per_s": 40.0,
+    return {"workload": "served-bump70-cyl30-split", "integrator": args.serve_integrator, "requests": R,
+            "arrival_rate_per_s": 40.0,
             "cells_range": [int(cells.min()), int(cells.max())], "cells_total": int(sum(m.n_cells for m in meshes)),
             "step_cap": cap, "resid_drop": 1e-8, "wall_s": wall, "solves_per_s": R / wall,
             "cell_updates_per_s": cu / wall, "latency_p50_s": float(np.percentile(lat, 50)),
             "latency_p99_s": float(np.percentile(lat, 99)), "latency_max_s": float(lat.max()),
             "statuses": sorted(set(int(done[k]["status"]) for k in range(R))),
+            "failed": [{"k": k, "kind": str(kinds[k]), "cells": meshes[k].n_cells, "status": int(done[k]["status"]),
+                        "iterations": int(done[k]["iterations"])} for k in range(R) if done[k]["status"] != 0],
             "done_reasons": {str(v): int((np.array([done[k]["done_reason"] for k in range(R)]) == v).sum())
                              for v in (0, 1, 2, 3)},
             "sequential_fp64": {"est_total_s": seq_s, "cell_updates_per_s": cu / seq_s,
@@ -600,6 +607,7 @@ def main():
     ap.add_argument("--requests", type=int, default=32)
     ap.add_argument("--max-cells", type=float, default=2e6)
     ap.add_argument("--step-cap", type=int, default=50000)
+    ap.add_argument("--serve-integrator", default="RK2", choices=["Euler", "RK2", "RK2_TVD", "RK4"])
     args = ap.parse_args()
     args.steps_given = "--steps" in sys.argv
     args.cells_given = "--cells" in sys.argv
