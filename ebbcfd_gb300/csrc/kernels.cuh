@@ -38,10 +38,11 @@ constexpr int BC_VERTICAL = 0x100;  // flag: reflection across a vertical edge (
 constexpr int ERR_NAN_EDGE = 8, ERR_NAN_CELL = 9, ERR_BC = 11;
 constexpr int UPD_THREADS = 256;
 
-// Minimum resident blocks per SM requested for the FP32 (split) kernels, which are
-// memory-latency bound: fewer registers per thread, more warps in flight.  Values
-// picked by ebbcfd_gb300/autotune.py (per-kernel event timing on GB300); the FP64
-// kernels are FP64-pipe bound and keep the compiler's register choice.
+// Minimum resident blocks per SM requested through __launch_bounds__ (a register cap
+// per thread: more warps in flight, possibly some spilling).  The FP32 (split)
+// kernels are memory-latency bound and gain from it; the FP64 kernels are FP64-pipe
+// bound.  Values picked by ebbcfd_gb300/autotune.py (per-kernel event timing on
+// GB300; 1 = the compiler's own register choice).
 #include "tuned.h"
 #ifndef EBB_CELL_MINB_F
 #define EBB_CELL_MINB_F 12
@@ -51,6 +52,15 @@ constexpr int UPD_THREADS = 256;
 #endif
 #ifndef EBB_UPD_MINB_F
 #define EBB_UPD_MINB_F 8
+#endif
+#ifndef EBB_CELL_MINB_D
+#define EBB_CELL_MINB_D 1
+#endif
+#ifndef EBB_FLUX_MINB_D
+#define EBB_FLUX_MINB_D 1
+#endif
+#ifndef EBB_UPD_MINB_D
+#define EBB_UPD_MINB_D 1
 #endif
 
 
@@ -297,7 +307,7 @@ __device__ __forceinline__ void lp_limit(const DMesh &M, int i, int ne, const T 
 }
 
 template <typename T, int MJ, bool LP>
-__global__ void __launch_bounds__(128, sizeof(T) == 4 ? EBB_CELL_MINB_F : 1) k_cell(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, int limit)
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? EBB_CELL_MINB_F : EBB_CELL_MINB_D) k_cell(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, int limit)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= M.C) return;
@@ -625,7 +635,7 @@ __device__ void boundary_flux(const DMesh &M, const DPhys &P, const DArrays &A, 
 }
 
 template <typename T>
-__global__ void __launch_bounds__(128, sizeof(T) == 4 ? EBB_FLUX_MINB_F : 1) k_flux(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, int nbi)
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? EBB_FLUX_MINB_F : EBB_FLUX_MINB_D) k_flux(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, int nbi)
 {
     if ((int)blockIdx.x >= nbi) {
         const int b = (blockIdx.x - nbi) * blockDim.x + threadIdx.x;
@@ -708,7 +718,7 @@ __device__ __forceinline__ float warp_maxf(float v)
 // integrators.d.  Split path: qin is the FP32 stage input, q64 is updated in FP64 and
 // the next stage input (qout) is its FP32 rounding.
 template <typename T, int ST>
-__global__ void __launch_bounds__(UPD_THREADS, sizeof(T) == 4 ? EBB_UPD_MINB_F : 1) k_update(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, T *qout,
+__global__ void __launch_bounds__(UPD_THREADS, sizeof(T) == 4 ? EBB_UPD_MINB_F : EBB_UPD_MINB_D) k_update(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, T *qout,
                                                        int dt_update, int need_dt, int final_stage)
 {
     constexpr bool SPLIT = sizeof(T) == 4;
