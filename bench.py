@@ -114,13 +114,13 @@ def peaks():
     return 6800.0, "fallback"
 
 
-PROFILED_CELLS = 994_095  # the wedge the committed ncu captures ran on
+PROFILED_CELLS = 1_001_045  # the wedge the committed ncu captures ran on
 
 
 def profiled_traffic(kernel, precision, ncell):
     """DRAM bytes (read + write) per launch of `kernel` from the committed ncu
     summaries under profiles/ ("traffic: <kernel> <precision> <bytes>" lines, one
-    capture of the 994,095-cell wedge), scaled to `ncell` cells (traffic grows with
+    capture of the 1,001,045-cell wedge), scaled to `ncell` cells (traffic grows with
     the cells processed); None when no capture covers the kernel."""
     import glob
     import re
@@ -327,6 +327,79 @@ def run_mms32(args):
     out["split_l2_rel_diff"] = abs(out["split"]["l2_rho"] / out["fp64"]["l2_rho"] - 1)
     for prec in ("fp64", "split"):
         del out[prec]["state"]
+    return out
+
+
+def shock_angle(xy, q, x_lo=0.8, x_hi=1.6, nbins=16, ramp_x=0.5):
+    """Angle (degrees) of the oblique shock from the ramp corner: in each x bin, the
+    highest cell whose pressure is above the midpoint of the freestream and
+    post-shock pressures marks the shock; a least-squares line through those points
+    (y = (x - x0) tan(beta)) gives beta."""
+    p = 0.4 * (q[:, 3] - 0.5 * (q[:, 1] ** 2 + q[:, 2] ** 2) / q[:, 0])
+    p_inf = 1.0 / (1.4 * 2.5 ** 2)
+    pts = []
+    edges = np.linspace(x_lo, x_hi, nbins + 1)
+    for a, b in zip(edges[:-1], edges[1:]):
+        m = (xy[:, 0] >= a) & (xy[:, 0] < b)
+        if not m.any():
+            continue
+        p2 = np.percentile(p[m], 95)
+        hi = m & (p > 0.5 * (p_inf + p2))
+        if hi.any():
+            pts.append((0.5 * (a + b), xy[hi, 1].max()))
+    x, y = np.array(pts).T
+    slope, icpt = np.polyfit(x, y, 1)
+    return float(np.degrees(np.arctan(slope))), float(-icpt / slope)
+
+
+def theory_shock_angle(M=2.5, theta_deg=15.0, g=1.4):
+    """Weak-shock solution of the theta-beta-Mach relation."""
+    th = np.radians(theta_deg)
+    best = None
+    for b in np.linspace(np.arcsin(1 / M) + 1e-6, np.pi / 2, 200001):
+        t = 2 / np.tan(b) * (M ** 2 * np.sin(b) ** 2 - 1) / (M ** 2 * (g + np.cos(2 * b)) + 2)
+        if t >= th:
+            best = b
+            break
+    return float(np.degrees(best))
+
+
+def run_wedge5000(args):
+    """Accuracy of configuration 2: the 1M-cell Mach 2.5 wedge run 5000 RK2 steps in
+    plain FP64 (bitwise equal to the oracle on the parity cases, and used here as the
+    reference solution: the oracle would take ~7 min on the host) and in split
+    precision; shock angle of both against the oblique-shock relation, and the split
+    path's L2 state error against FP64."""
+    import ctypes as C
+    import ebbcfd_gb300 as E
+    from ebbcfd_gb300 import _lib, meshgen
+    L = _lib.load()
+    steps = args.steps if args.steps_given else 5000
+    mesh = meshgen.wedge(args.cells, seed=0).to_solver_mesh()
+    xy = mesh.centroids()
+    out = {"workload": "wedge-M2.5-rusanov-rk2-cfl0.4-accuracy", "cells": mesh.n_cells, "steps": steps,
+           "theory_shock_angle_deg": theory_shock_angle()}
+    qs = {}
+    for prec in ("fp64", "split"):
+        s = E.UfvmSolver(mesh, E.load_config(wedge_config()), precision=prec)
+        n = C.c_int64()
+        ms = C.c_double()
+        code = L.ebb_run_timed(s.h, steps, C.byref(n), C.byref(ms))
+        if code:
+            s._raise(code)
+        q = s.state
+        qs[prec] = q
+        t_end = s.time()[0]
+        # the corner shock is established within about the distance the flow has moved
+        span = min(1.1, 0.9 * t_end)
+        beta, x0 = shock_angle(xy, q, x_lo=0.5 + 0.15 * span, x_hi=0.5 + 0.85 * span, nbins=10)
+        out[prec] = {"cell_updates_per_s": mesh.n_cells * n.value / (ms.value / 1e3), "shock_angle_deg": beta,
+                     "shock_origin_x": x0, "t": t_end, "shock_window_x": [0.5 + 0.15 * span, 0.5 + 0.85 * span]}
+        s.close()
+    d = qs["split"] - qs["fp64"]
+    out["split_l2_rel_err"] = [float(np.sqrt(np.mean(d[:, k] ** 2)) / np.sqrt(np.mean(qs["fp64"][:, k] ** 2)))
+                               for k in range(4)]
+    out["split_max_rel_err"] = float((np.abs(d).max(axis=0) / np.abs(qs["fp64"]).max(axis=0)).max())
     return out
 
 
@@ -600,7 +673,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-split", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
-    ap.add_argument("--workload", default="wedge", choices=["wedge", "mms32", "plate4m", "batch512", "serve"])
+    ap.add_argument("--workload", default="wedge",
+                    choices=["wedge", "wedge5000", "mms32", "plate4m", "batch512", "serve"])
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--seq-stride", type=int, default=4)
     ap.add_argument("--seq-steps", type=int, default=100)
@@ -615,7 +689,8 @@ def main():
     ws, rank, local = dist_env()
     if args.workload != "wedge":
         # accuracy/throughput reports for the other configurations (not the headline line)
-        run = {"mms32": run_mms32, "plate4m": run_plate, "batch512": run_batch512, "serve": run_serve}
+        run = {"mms32": run_mms32, "plate4m": run_plate, "batch512": run_batch512, "serve": run_serve,
+               "wedge5000": run_wedge5000}
         out = run[args.workload](args)
         print(json.dumps(out))
         return

@@ -7,8 +7,8 @@ element numbers, line elements (type 1) carrying the physical tag as the first t
 tags 1..N in PhysicalNames order, triangles type 2, quads type 3.
 
 * ``wedge``: [0,3]x[0,1] minus the 15-degree ramp from x=0.5; triangles from a
-  seeded Delaunay triangulation of jittered points whose spacing is graded 2x finer
-  toward the ramp.  Tags: Inflow (x=0), Top (y=1), Symmetry (y=0, x<0.5), Ramp,
+  seeded Delaunay triangulation of Poisson-disk points whose spacing is graded 2x
+  finer toward the ramp.  Tags: Inflow (x=0), Top (y=1), Symmetry (y=0, x<0.5), Ramp,
   Outflow (x=3).
 * ``bump_channel``: [0,3]x[0,1] with a bump y = h sin^2(pi (x-1)) on 1<=x<=2;
   Delaunay triangles.  Tags: Inflow, Outflow, Wall.
@@ -160,6 +160,47 @@ def _interior_points(rng, xlo, xhi, ylo, yhi, h_fn, inside, h0):
     return np.column_stack([x[m], y[m]])
 
 
+def _poisson_points(rng, xlo, xhi, ylo, yhi, h_fn, inside, h0, rho):
+    """Poisson-disk points with local radius rho h(x, y): a jittered candidate grid
+    (spacing 0.75 h0) reduced to a maximal independent set of the graph joining
+    candidates closer than rho times their mean local spacing (Luby's random-priority
+    rounds), then kept at least half a local spacing inside the boundary."""
+    from scipy.spatial import cKDTree
+    s = 0.75 * h0
+    nx = int(math.ceil((xhi - xlo) / s))
+    ny = int(math.ceil((yhi - ylo) / s))
+    gx, gy = np.meshgrid((np.arange(nx) + 0.5) * s + xlo, (np.arange(ny) + 0.5) * s + ylo)
+    x = gx.ravel() + rng.uniform(-0.4, 0.4, gx.size) * s
+    y = gy.ravel() + rng.uniform(-0.4, 0.4, gy.size) * s
+    m = inside(x, y, 0.5 * h_fn(x, y))
+    x, y = x[m], y[m]
+    h = h_fn(x, y)
+    pts = np.column_stack([x, y])
+    pairs = cKDTree(pts).query_pairs(rho * float(h.max()), output_type="ndarray")
+    i, j = pairs[:, 0], pairs[:, 1]
+    d = np.hypot(x[i] - x[j], y[i] - y[j])
+    close = d < rho * 0.5 * (h[i] + h[j])
+    i, j = i[close], j[close]
+    n = len(x)
+    prio = rng.permutation(n)
+    alive = np.ones(n, bool)
+    kept = np.zeros(n, bool)
+    while True:
+        a = alive[i] & alive[j]
+        ii, jj = i[a], j[a]
+        if len(ii) == 0:
+            kept |= alive
+            break
+        lose = np.zeros(n, bool)
+        lose[np.where(prio[ii] < prio[jj], ii, jj)] = True
+        win = alive & ~lose
+        kept |= win
+        alive &= ~win
+        alive[jj[win[ii]]] = False
+        alive[ii[win[jj]]] = False
+    return pts[kept]
+
+
 def wedge(n_cells=1_000_000, seed=0, angle_deg=15.0, ramp_x=0.5):
     rng = np.random.default_rng(seed)
     ta = math.tan(math.radians(angle_deg))
@@ -196,7 +237,16 @@ def wedge(n_cells=1_000_000, seed=0, angle_deg=15.0, ramp_x=0.5):
     def inside(x, y, margin):
         return (x > margin) & (x < 3.0 - margin) & (y < 1.0 - margin) & (y - floor_y(x) > margin * 1.05)
 
-    ip = _interior_points(rng, 0.0, 3.0, 0.0, 1.0, h_fn, inside, hc)
+    # Poisson-disk interior points; the point count goes as rho^-1.74 (measured), and
+    # rho = 0.71 puts the triangle count near n_cells; a second pass corrects it when
+    # it is off by more than 2%
+    rho = 0.71
+    for _ in range(2):
+        ip = _poisson_points(np.random.default_rng(seed), 0.0, 3.0, 0.0, 1.0, h_fn, inside, hc, rho)
+        ratio = (2 * len(ip) + len(bpts)) / n_cells
+        if abs(ratio - 1) < 0.02:
+            break
+        rho *= ratio ** (1 / 1.74)
     nodes = np.vstack([bpts, ip])
     tri = Delaunay(nodes).simplices.astype(np.int64)
     tris, a = _ccw(nodes, tri)
