@@ -162,3 +162,37 @@ def test_save_load_roundtrip(tmp_path):
     assert np.array_equal(sol2.state, q)
     t2, dt2, _ = sol2.time()
     assert (t2, dt2) == (t, dt)
+
+
+def _write_esln_part(path, ids, q, t, dt, nedges):
+    """.esln v2 holding only the cells `ids` (one rank's file of a partitioned run,
+    io.d:68-161): global id, edge count, state, zero face states, then 4 CRC bytes."""
+    import struct
+    b = bytearray(struct.pack(">III", 0xEA98E1F5, 2, len(ids)) + struct.pack(">dd", t, dt) + struct.pack(">II", 4, 2))
+    for i in ids:
+        b += struct.pack(">IB", int(i), int(nedges[i])) + struct.pack(">4d", *q[i]) + bytes(32 * int(nedges[i]))
+    b += bytes(4)
+    open(path, "wb").write(bytes(b))
+
+
+def test_load_solution_parts_places_cells_by_global_id(tmp_path):
+    sol, om = case("mms_tri_limited").build()
+    sol.run(3)
+    q = sol.state
+    t, dt, _ = sol.time()
+    n = len(q)
+    nedges = np.full(n, 3)
+    rng = np.random.default_rng(0)
+    perm = rng.permutation(n)
+    parts = [perm[: n // 3], perm[n // 3:]]  # two "ranks", cells in arbitrary order
+    paths = []
+    for r, ids in enumerate(parts):
+        p = tmp_path / ("save_0_%d.esln" % r)
+        _write_esln_part(p, ids, q, t if r == 0 else 0.0, dt if r == 0 else 0.0, nedges)
+        paths.append(str(p))
+    sol2, _ = case("mms_tri_limited").build()
+    sol2.load_solution_parts(paths)
+    assert np.array_equal(sol2.state, q)
+    assert sol2.time()[:2] == (t, dt)  # from the first file
+    with pytest.raises(E.EbbError):  # one rank's file alone leaves cells uncovered
+        sol2.load_solution_parts(paths[1:])
