@@ -391,7 +391,58 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? EBB_CELL_MINB_F : EBB_CE
     }
     }
     T lim0[4] = {T(1.0), T(1.0), T(1.0), T(1.0)}, lim1[4] = {T(1.0), T(1.0), T(1.0), T(1.0)};
-    if (second && P.limited && limit) {
+    if (second && P.limited && limit && sizeof(T) == 8) {
+        // FP64: the out-of-bounds tests first, then only the needed divisions in a
+        // compact loop.  Branching on each (neighbour, component) pair makes a warp run
+        // a division whenever any of its lanes needs it, and an FP64 division costs
+        // about ten FP64-unit instructions per warp; the compact loop runs as many as
+        // the busiest lane needs.  Each component's limiter still takes the minimum in
+        // neighbour order (pairs in bounds give s = 1, which leaves it unchanged).
+        unsigned need = 0, above = 0;
+#pragma unroll
+        for (int j = 0; j < MJ; j++) {
+            if (j < ne) {
+                const typename V2<T>::t nd = ld2<T>(M.g.s_nd, (size_t)j * Cs + i);
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const T qE = qi[k] + (g[k][0] * nd.x + g[k][1] * nd.y);
+                    const unsigned bit = 1u << (4 * j + k);
+                    if (qE < mn[k])
+                        need |= bit;
+                    else if (qE > mx[k]) {
+                        need |= bit;
+                        above |= bit;
+                    }
+                }
+            }
+        }
+        while (need) {
+            const int t = __ffs(need) - 1;
+            const unsigned bit = 1u << t;
+            need &= need - 1;
+            const int j = t >> 2, k = t & 3;
+            const typename V2<T>::t nd = ld2<T>(M.g.s_nd, (size_t)j * Cs + i);
+            T g0 = g[0][0], g1 = g[0][1], q = qi[0], lo = mn[0], hi = mx[0], l = lim0[0];
+#pragma unroll
+            for (int kk = 1; kk < 4; kk++)
+                if (k == kk) {
+                    g0 = g[kk][0];
+                    g1 = g[kk][1];
+                    q = qi[kk];
+                    lo = mn[kk];
+                    hi = mx[kk];
+                    l = lim0[kk];
+                }
+            const T s = ((above & bit) ? hi - q : lo - q) / (g0 * nd.x + g1 * nd.y);
+            l = fmin(l, s);
+#pragma unroll
+            for (int kk = 0; kk < 4; kk++)
+                if (k == kk) lim0[kk] = l;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) lim1[k] = lim0[k];
+        if (LP) lp_limit<T>(M, i, ne, qi, mn, mx, g, lim0, lim1, (T)P.lp_thresh);
+    } else if (second && P.limited && limit) {
 #pragma unroll
         for (int j = 0; j < MJ; j++) {
             if (j < ne) {
