@@ -351,6 +351,9 @@ Dims dims_of(const std::vector<InstLayout> &Ls)
         D.any_mms |= L.cfg.mms != 0;
         D.nblk += (int)((L.C + UPD - 1) / UPD);
     }
+    // slot rows up to the kernels' compiled neighbour count (3, 4 or 6): the stage
+    // kernels load every row unconditionally and select by the cell's edge count
+    D.MJ = D.MJ <= 3 ? 3 : (D.MJ == 4 ? 4 : 6);
     D.Cs = (D.Ct + 31) & ~(int64_t)31;
     if (D.n == 1) D.nblk = update_blocks((int)D.Ct);
     return D;

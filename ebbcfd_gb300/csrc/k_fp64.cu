@@ -23,6 +23,8 @@ template <typename T> __global__ void __launch_bounds__(EBB_RED_THREADS) k_step_
     const int b0 = M.inst_blk ? M.inst_blk[inst] : 0, b1 = M.inst_blk ? M.inst_blk[inst + 1] : nblk;
     const int fb0 = M.force_off ? M.force_off[inst] : 0, fb1 = M.force_off ? M.force_off[inst + 1] : M.n_force;
     const int ncell = M.inst_c0 ? M.inst_c0[inst + 1] - M.inst_c0[inst] : M.C;
+    grid_dep_release();
+    grid_dep_wait();
     if (st->done) return;
     if (st->err_key != EBB_NOERR) {
         if (threadIdx.x == 0) st->done = 1;
@@ -156,11 +158,12 @@ int update_grid(const DMesh &M) { return M.n_upd_blocks; }
 int launch_step_end(const DMesh &M, const DArrays &A, int nred_blocks, int split, void *stream)
 {
     const int n = M.n_inst > 0 ? M.n_inst : 1;
+    cudaError_t e;
     if (split)
-        k_step_end<float><<<n, EBB_RED_THREADS, 0, (cudaStream_t)stream>>>(M, A, nred_blocks);
+        e = launch_dep(k_step_end<float>, dim3(n), dim3(EBB_RED_THREADS), (cudaStream_t)stream, M, A, nred_blocks);
     else
-        k_step_end<double><<<n, EBB_RED_THREADS, 0, (cudaStream_t)stream>>>(M, A, nred_blocks);
-    return ret(cudaGetLastError());
+        e = launch_dep(k_step_end<double>, dim3(n), dim3(EBB_RED_THREADS), (cudaStream_t)stream, M, A, nred_blocks);
+    return ret(e);
 }
 
 int launch_flux_batch(int kind, int64_t n, const double *qL, const double *qR, const double *nrm, double *F, double *s,

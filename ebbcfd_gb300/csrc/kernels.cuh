@@ -27,6 +27,7 @@
 #include <math.h>
 #include <stdint.h>
 
+#include "bitconv.h"
 #include "device_math.cuh"
 #include "layout.h"
 
@@ -70,6 +71,45 @@ __device__ __forceinline__ void flag_error(DState *st, unsigned phase, unsigned 
 {
     unsigned long long key = ((unsigned long long)phase << 48) | ((unsigned long long)code << 40) | idx;
     atomicMin(&st->err_key, key);
+}
+
+// Programmatic dependent launch.  The stage kernels and the step epilogue are
+// launched with programmatic stream serialisation: a kernel's blocks may start while
+// the previous kernel's last blocks still run, load the read-only mesh arrays (slot
+// indices, geometry), and then wait at grid_dep_wait() until the previous kernel has
+// completed and its writes are visible.  Every thread passes the wait before its
+// first access to data another kernel writes and before it exits, so completion of a
+// kernel implies completion of all kernels before it.  grid_dep_release() lets the
+// next kernel start launching once every block of this one has issued it; it orders
+// nothing.  In a launch without the attribute the wait returns at once.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KP, typename... AP>
+inline cudaError_t launch_dep(void (*kernel)(KP...), dim3 grid, dim3 block, cudaStream_t s, AP... args)
+{
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t c = {};
+    c.gridDim = grid;
+    c.blockDim = block;
+    c.dynamicSmemBytes = 0;
+    c.stream = s;
+    c.attrs = at;
+    c.numAttrs = 1;
+    return cudaLaunchKernelEx(&c, kernel, args...);
+}
+
+// FP32 <-> FP64 conversions on the integer pipe (bitconv.h), for the split path
+__device__ __forceinline__ double f2d_int(float x)
+{
+    const uint64_t b = ebbbits::f2d_bits(__float_as_uint(x));
+    return __hiloint2double((int)(uint32_t)(b >> 32), (int)(uint32_t)b);
+}
+__device__ __forceinline__ float d2f_int(double x)
+{
+    return __uint_as_float(ebbbits::d2f_bits((uint32_t)__double2hiint(x), (uint32_t)__double2loint(x)));
 }
 
 // 4-vector loads/stores: two 16-byte accesses for double, one for float
@@ -310,14 +350,37 @@ template <typename T, int MJ, bool LP>
 __global__ void __launch_bounds__(128, sizeof(T) == 4 ? EBB_CELL_MINB_F : EBB_CELL_MINB_D) k_cell(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, int limit)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= M.C) return;
-    DState *st = A.st + (M.cell_inst ? M.cell_inst[i] : 0);
-    if (halted(st)) return;
+    const bool act = i < M.C;
     const int Cs = M.Cs;
+    // read-only mesh data first, before the wait for the previous kernel.  Split path:
+    // the neighbour rows are loaded whatever the cell's edge count (rows past it hold
+    // 0), and the limiter's and the reconstruction's geometry (neighbour and face
+    // midpoint offsets) is loaded here, not behind the gathers
+    int ne = 0, inst = 0;
+    int nbv[MJ];
+    typename V2<T>::t gmv[MJ], ndv[MJ], fdv[MJ];
+    if (act) {
+        ne = M.nedge[i];
+        if (M.cell_inst) inst = M.cell_inst[i];
+        if constexpr (sizeof(T) == 4) {
+#pragma unroll
+            for (int j = 0; j < MJ; j++) nbv[j] = M.s_nbr[(size_t)j * Cs + i];
+#pragma unroll
+            for (int j = 0; j < MJ; j++) {
+                gmv[j] = ld2<T>(M.g.s_gm, (size_t)j * Cs + i);
+                ndv[j] = ld2<T>(M.g.s_nd, (size_t)j * Cs + i);
+                fdv[j] = ld2<T>(M.g.s_fd, (size_t)j * Cs + i);
+            }
+        }
+    }
+    grid_dep_release();
+    grid_dep_wait();
+    if (!act) return;
+    DState *st = A.st + inst;
+    if (halted(st)) return;
     T *qghost = const_cast<T *>(qin);  // ghost slots [C, C+G) are written by their owner only
     T qi[4];
     ld4(qin + 4 * (size_t)i, qi);
-    const int ne = M.nedge[i];
     T mn[4], mx[4], g[4][2];
 #pragma unroll
     for (int k = 0; k < 4; k++) {
@@ -327,23 +390,13 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? EBB_CELL_MINB_F : EBB_CE
         g[k][1] = T(0.0);
     }
     const bool second = P.order > 1;
-    // split path: the limiter's and the reconstruction's geometry (neighbour and face
-    // midpoint offsets) is loaded with the first wave of loads, not behind the gathers
-    typename V2<T>::t ndv[MJ], fdv[MJ];
     if constexpr (sizeof(T) == 4) {
-        // all index and neighbour-state loads in flight before any dependent math
-        int nbv[MJ];
+        // all neighbour-state gathers in flight before any dependent math
         T qv[MJ][4];
-        typename V2<T>::t gmv[MJ];
 #pragma unroll
-        for (int j = 0; j < MJ; j++) nbv[j] = (j < ne) ? M.s_nbr[(size_t)j * Cs + i] : i;
+        for (int j = 0; j < MJ; j++) nbv[j] = (j < ne) ? nbv[j] : i;
 #pragma unroll
-        for (int j = 0; j < MJ; j++) {
-            ld4(qin + 4 * (size_t)(nbv[j] < M.C ? nbv[j] : i), qv[j]);
-            gmv[j] = ld2<T>(M.g.s_gm, (size_t)j * Cs + i);
-            ndv[j] = ld2<T>(M.g.s_nd, (size_t)j * Cs + i);
-            fdv[j] = ld2<T>(M.g.s_fd, (size_t)j * Cs + i);
-        }
+        for (int j = 0; j < MJ; j++) ld4(qin + 4 * (size_t)(nbv[j] < M.C ? nbv[j] : i), qv[j]);
 #pragma unroll
         for (int j = 0; j < MJ; j++) {
             if (j < ne) {
@@ -689,22 +742,34 @@ template <typename T>
 __global__ void __launch_bounds__(128, sizeof(T) == 4 ? EBB_FLUX_MINB_F : EBB_FLUX_MINB_D) k_flux(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, int nbi)
 {
     if ((int)blockIdx.x >= nbi) {
+        grid_dep_release();
+        grid_dep_wait();
         const int b = (blockIdx.x - nbi) * blockDim.x + threadIdx.x;
         if (b < M.G) boundary_flux<T>(M, P, A, qin, b);
         return;
     }
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= M.Eint) return;
+    const bool act = e < M.Eint;
+    // read-only mesh data before the wait for the previous kernel
     int inst = 0;
-    if (M.cell_inst) inst = M.cell_inst[reinterpret_cast<const int2 *>(M.e_cell)[e].x];
+    int2 sl = make_int2(0, 0);
+    typename V2<T>::t n = {};
+    T len = T(0.0);
+    if (act) {
+        if (M.cell_inst) inst = M.cell_inst[reinterpret_cast<const int2 *>(M.e_cell)[e].x];
+        sl = reinterpret_cast<const int2 *>(M.e_slot)[e];
+        n = ld2<T>(M.g.e_n, e);
+        len = ld1<T>(M.g.e_len, e);
+    }
+    grid_dep_release();
+    grid_dep_wait();
+    if (!act) return;
     DState *st = A.st + inst;
     if (halted(st)) return;
-    const int2 sl = reinterpret_cast<const int2 *>(M.e_slot)[e];
     const T *face = reinterpret_cast<const T *>(A.face);
     T qL[4], qR[4], F[4], sMax;
     ld4(face + 4 * (size_t)sl.x, qL);
     ld4(face + 4 * (size_t)sl.y, qR);
-    const typename V2<T>::t n = ld2<T>(M.g.e_n, e);
     inviscid_flux(P.flux, qL, qR, n.x, n.y, F, sMax);
     if (P.viscous) {
         const int2 c = reinterpret_cast<const int2 *>(M.e_cell)[e];
@@ -720,7 +785,6 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? EBB_FLUX_MINB_F : EBB_FL
         for (int k = 0; k < 4; k++) F[k] = F[k] - Fv[k];
     }
     if (has_nan(F)) flag_error(st, 2, ERR_NAN_EDGE, (unsigned)M.e_ref[e]);
-    const T len = ld1<T>(M.g.e_len, e);
     T lf[4] = {len * F[0], len * F[1], len * F[2], len * F[3]};
     st4(reinterpret_cast<T *>(A.fl) + 4 * (size_t)e, lf);
     reinterpret_cast<T *>(A.fs)[e] = len * sMax;
@@ -768,7 +832,7 @@ __device__ __forceinline__ float warp_maxf(float v)
 // FP64 for both precision forms.  FP64 path: qin/qout are double stage states as in
 // integrators.d.  Split path: qin is the FP32 stage input, q64 is updated in FP64 and
 // the next stage input (qout) is its FP32 rounding.
-template <typename T, int ST>
+template <typename T, int ST, int MJ>
 __global__ void __launch_bounds__(UPD_THREADS, sizeof(T) == 4 ? EBB_UPD_MINB_F : EBB_UPD_MINB_D) k_update(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, T *qout,
                                                        int dt_update, int need_dt, int final_stage)
 {
@@ -782,34 +846,52 @@ __global__ void __launch_bounds__(UPD_THREADS, sizeof(T) == 4 ? EBB_UPD_MINB_F :
         i = blockIdx.x * blockDim.x + threadIdx.x;
         iend = M.C;
     }
+    const bool act = i < iend;
+    const int Cs = M.Cs;
+    // read-only mesh data before the wait for the previous kernel: every edge row is
+    // loaded whatever the cell's edge count (rows past it hold 0)
+    int ev[MJ], ne = 0;
+    if (act) {
+#pragma unroll
+        for (int j = 0; j < MJ; j++) ev[j] = M.s_edge[(size_t)j * Cs + i];
+        ne = M.nedge[i];
+    }
+    grid_dep_release();
+    grid_dep_wait();
     DState *st = A.st + inst;
     if (halted(st)) return;
-    const bool act = i < iend;
     double dtc = INFINITY, rm = 0.0;
     double ss[4] = {0, 0, 0, 0}, vs[4] = {0, 0, 0, 0};
     float fss[4] = {0, 0, 0, 0}, fvs[4] = {0, 0, 0, 0};  // split path: FP32 lane values
     float fdtc = INFINITY, frm = 0.0f;
     bool bad = false;
     if (act) {
-        const int Cs = M.Cs;
-        const int ne = M.nedge[i];
+        // all flux gathers are issued before the sums, which add in edge order
         const T *fl = reinterpret_cast<const T *>(A.fl);
         const T *fs = reinterpret_cast<const T *>(A.fs);
+        T f[MJ][4], fe[MJ];
+#pragma unroll
+        for (int j = 0; j < MJ; j++) {
+            if (j < ne) {
+                const size_t e = (size_t)(ev[j] & 0x7fffffff);
+                ld4(fl + 4 * e, f[j]);
+                fe[j] = fs[e];
+            }
+        }
         T r[4] = {T(0.0), T(0.0), T(0.0), T(0.0)};
         T sAve = 0;
-        for (int j = 0; j < ne; j++) {
-            const int ev = M.s_edge[(size_t)j * Cs + i];
-            const size_t e = (size_t)(ev & 0x7fffffff);
-            T f[4];
-            ld4(fl + 4 * e, f);
-            if (ev < 0) {
 #pragma unroll
-                for (int k = 0; k < 4; k++) r[k] = r[k] + (-f[k]);
-            } else {
+        for (int j = 0; j < MJ; j++) {
+            if (j < ne) {
+                if (ev[j] < 0) {
 #pragma unroll
-                for (int k = 0; k < 4; k++) r[k] = r[k] + f[k];
+                    for (int k = 0; k < 4; k++) r[k] = r[k] + (-f[j][k]);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 4; k++) r[k] = r[k] + f[j][k];
+                }
+                sAve += fe[j];
             }
-            sAve += fs[e];
         }
         T *cdt = reinterpret_cast<T *>(A.cdt);
         if (need_dt || (P.local_ts && dt_update)) {
@@ -892,12 +974,14 @@ __global__ void __launch_bounds__(UPD_THREADS, sizeof(T) == 4 ? EBB_UPD_MINB_F :
             }
             T o[4];
             if (final_stage) {
+                // u += inc in FP64; the conversions run on the integer pipe (an FP64
+                // conversion costs about as much FP64-pipe time as the add)
                 double q0[4], out[4];
                 ld4(A.q64 + 4 * (size_t)i, q0);
 #pragma unroll
                 for (int k = 0; k < 4; k++) {
-                    out[k] = q0[k] + (double)inc[k];
-                    o[k] = (T)out[k];
+                    out[k] = q0[k] + f2d_int(inc[k]);
+                    o[k] = d2f_int(out[k]);
                 }
                 st4(A.q64 + 4 * (size_t)i, out);
 #pragma unroll
@@ -1111,11 +1195,12 @@ int launch_cell_impl(const DMesh &M, const DPhys &P, const DArrays &A, const T *
     if (grid.x == 0) return 0;
     cudaStream_t s = (cudaStream_t)stream;
     const bool lp = P.lp && P.limited;
-#define EBB_CELL(MJ)                                                          \
-    if (lp)                                                                   \
-        k_cell<T, MJ, true><<<grid, TB, 0, s>>>(M, P, A, qin, limit);         \
-    else                                                                      \
-        k_cell<T, MJ, false><<<grid, TB, 0, s>>>(M, P, A, qin, limit);
+    cudaError_t e;
+#define EBB_CELL(MJ)                                                              \
+    if (lp)                                                                       \
+        e = launch_dep(k_cell<T, MJ, true>, grid, dim3(TB), s, M, P, A, qin, limit); \
+    else                                                                          \
+        e = launch_dep(k_cell<T, MJ, false>, grid, dim3(TB), s, M, P, A, qin, limit);
     if (M.maxJ <= 3) {
         EBB_CELL(3)
     } else if (M.maxJ == 4) {
@@ -1124,7 +1209,7 @@ int launch_cell_impl(const DMesh &M, const DPhys &P, const DArrays &A, const T *
         EBB_CELL(6)
     }
 #undef EBB_CELL
-    return ret(cudaGetLastError());
+    return ret(e);
 }
 
 template <typename T> int launch_flux_impl(const DMesh &M, const DPhys &P, const DArrays &A, const T *qin, void *stream)
@@ -1132,8 +1217,7 @@ template <typename T> int launch_flux_impl(const DMesh &M, const DPhys &P, const
     const int TB = 128;
     int nbi = (M.Eint + TB - 1) / TB, nbb = (M.G + TB - 1) / TB;
     if (nbi + nbb == 0) return 0;
-    k_flux<T><<<nbi + nbb, TB, 0, (cudaStream_t)stream>>>(M, P, A, qin, nbi);
-    return ret(cudaGetLastError());
+    return ret(launch_dep(k_flux<T>, dim3(nbi + nbb), dim3(TB), (cudaStream_t)stream, M, P, A, qin, nbi));
 }
 
 template <typename T>
@@ -1143,9 +1227,17 @@ int launch_update_impl(const DMesh &M, const DPhys &P, const DArrays &A, int sta
     dim3 grid(M.n_upd_blocks);
     if (grid.x == 0) return 0;
     cudaStream_t s = (cudaStream_t)stream;
-#define EBB_UPD(S)                                                                                       \
-    case S:                                                                                              \
-        k_update<T, S><<<grid, UPD_THREADS, 0, s>>>(M, P, A, qin, qout, dt_update, need_dt, final_stage); \
+    cudaError_t e = cudaSuccess;
+#define EBB_UPD_MJ(S, MJ) \
+    e = launch_dep(k_update<T, S, MJ>, grid, dim3(UPD_THREADS), s, M, P, A, qin, qout, dt_update, need_dt, final_stage)
+#define EBB_UPD(S)                  \
+    case S:                         \
+        if (M.maxJ <= 3)            \
+            EBB_UPD_MJ(S, 3);       \
+        else if (M.maxJ == 4)       \
+            EBB_UPD_MJ(S, 4);       \
+        else                        \
+            EBB_UPD_MJ(S, 6);       \
         break;
     switch (stage) {
         EBB_UPD(ST_RESID)
@@ -1162,7 +1254,8 @@ int launch_update_impl(const DMesh &M, const DPhys &P, const DArrays &A, int sta
         return -1;
     }
 #undef EBB_UPD
-    return ret(cudaGetLastError());
+#undef EBB_UPD_MJ
+    return ret(e);
 }
 
 // ---- ebb-reconstruct (app/reconstruct.d:239-424) --------------------------------

@@ -482,3 +482,53 @@ def uniform_quads(n=32):
     for i in range(n, 0, -1):
         b.append((qid[i, 0], qid[i - 1, 0]))
     return MeshArrays(nodes, quads + 1, np.array(b), [0], ["Freestream"])
+
+
+def hanging_quads(n=16):
+    """Non-conforming quads on [0,1]^2: an n x n grid (n even) whose cells with
+    x index >= n/2 or y index >= n/2 are split 2 x 2.  The unsplit cells next to
+    split ones carry the split side's middle node, so the mesh has pentagons along
+    both interfaces and a hexagon at their corner (the reference's cells have up to
+    six edges, source/mesh.d:26).  One tag (Freestream)."""
+    assert n % 2 == 0 and n >= 4
+    m = 2 * n + 1
+    fid = lambda a, b: b * m + a  # noqa: E731  (fine-grid node id)
+    split = lambda i, j: i >= n // 2 or j >= n // 2  # noqa: E731
+    rows = []
+    for j in range(n):
+        for i in range(n):
+            if split(i, j):
+                for b in (2 * j, 2 * j + 1):
+                    for a in (2 * i, 2 * i + 1):
+                        rows.append([fid(a, b), fid(a + 1, b), fid(a + 1, b + 1), fid(a, b + 1)])
+            else:
+                v = [fid(2 * i, 2 * j), fid(2 * i + 2, 2 * j)]
+                if i + 1 < n and split(i + 1, j):
+                    v.append(fid(2 * i + 2, 2 * j + 1))
+                v.append(fid(2 * i + 2, 2 * j + 2))
+                if j + 1 < n and split(i, j + 1):
+                    v.append(fid(2 * i + 1, 2 * j + 2))
+                v.append(fid(2 * i, 2 * j + 2))
+                rows.append(v)
+    b = []
+    for i in range(n):  # counter-clockwise walk: bottom, right, top, left
+        b += [(fid(2 * i, 0), fid(2 * i + 1, 0)), (fid(2 * i + 1, 0), fid(2 * i + 2, 0))] if split(i, 0) \
+            else [(fid(2 * i, 0), fid(2 * i + 2, 0))]
+    b += [(fid(2 * n, k), fid(2 * n, k + 1)) for k in range(2 * n)]
+    b += [(fid(k, 2 * n), fid(k - 1, 2 * n)) for k in range(2 * n, 0, -1)]
+    for j in range(n - 1, -1, -1):
+        b += [(fid(0, 2 * j + 2), fid(0, 2 * j + 1)), (fid(0, 2 * j + 1), fid(0, 2 * j))] if split(0, j) \
+            else [(fid(0, 2 * j + 2), fid(0, 2 * j))]
+    used = np.unique(np.concatenate([np.asarray(r) for r in rows]))
+    new = np.full(m * m, -1, dtype=np.int64)
+    new[used] = np.arange(len(used))
+    xs = np.linspace(0.0, 1.0, m)
+    nodes = np.column_stack([xs[used % m], xs[used // m]])
+    blocks, run = [], []
+    for r in rows:  # consecutive cells with the same edge count form one block
+        if run and len(run[-1]) != len(r):
+            blocks.append(np.asarray(run, dtype=np.int64) + 1)
+            run = []
+        run.append([int(new[v]) for v in r])
+    blocks.append(np.asarray(run, dtype=np.int64) + 1)
+    return MeshArrays(nodes, blocks, new[np.asarray(b)], [0], ["Freestream"])

@@ -98,6 +98,11 @@ def all_cases():
              text=cfg_json(initialConditions=[0.5, 0, 1, 1], integrator="RK2_TVD",
                            boudaryConditions=[{"tag": "Freestream", "type": "dirichlet", "q": [0.5, 0, 1, 1]}],
                            CFL=0.5), mms=2),
+        # pentagons and a hexagon (hanging nodes): the six-neighbour kernels
+        Case("hanging_polygons_rk2", gen=lambda: meshgen.hanging_quads(16),
+             text=cfg_json(initialConditions=[0.5, 0, 1, 1], integrator="RK2",
+                           boudaryConditions=[{"tag": "Freestream", "type": "dirichlet", "q": [0.5, 0, 1, 1]}],
+                           CFL=0.5), mms=2),
         Case("order1_local_dt", "ms_refine_tri_1.msh",
              text=mms_text("ms_refine_3.json", order=1, localTimestep=True, lpThresh=-1), mms=1),
     ]

@@ -137,3 +137,33 @@ def test_footprint_matches_allocation(instances):
     fp = E.batch_footprint(meshes, cfgs, "split")
     one = sum(E.batch_footprint([m], [c], "split") for m, c in zip(meshes, cfgs))
     assert 0.8 * one < fp < 1.2 * one
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_triangles_batched_with_polygons(instances, precision):
+    """A triangle mesh batched with a mesh of quads, pentagons and a hexagon runs
+    through the six-neighbour kernels (the padded slot rows of its cells are never
+    used) and still gives bitwise its own three-neighbour solve."""
+    meshes, cfgs = instances
+    poly = meshgen.hanging_quads(12).to_solver_mesh()
+    q = [0.5, 0, 1, 1]
+    pcfg = E.load_config(json.dumps({
+        "mesh": "m.msh", "dt": 1e-4, "tEnd": 1000.0, "flux": "roeFlux", "saveIter": -1, "plotIter": -1,
+        "forceBoundary": "Freestream", "initialConditions": q, "integrator": "RK2_TVD", "CFL": 0.5,
+        "boudaryConditions": [{"tag": "Freestream", "type": "fullState", "q": q}]}))
+    qp = E.UfvmSolver(poly, pcfg, precision)
+    rng = np.random.default_rng(3)
+    start = qp.state * (1 + 0.02 * rng.uniform(-1, 1, qp.state.shape))  # a flow that moves
+    qp.close()
+    b = E.UfvmBatch([meshes[0], poly], [cfgs[0], pcfg], precision)
+    b.set_instance_state(1, start)
+    b.run(25, records=False)
+    q0, _, _ = single_run(meshes[0], cfgs[0], 25, precision)
+    assert np.array_equal(b.instance_state(0), q0)
+    s = E.UfvmSolver(poly, pcfg, precision)
+    s.set_state(start)
+    s.run(25, records=False)
+    assert np.array_equal(b.instance_state(1), s.state)
+    assert np.abs(s.state - start).max() > 0
+    s.close()
+    b.close()

@@ -308,3 +308,69 @@ def test_bump_channel_mesh_follows_the_bump():
     a = 0.5 * ((p[:, 1, 0] - p[:, 0, 0]) * (p[:, 2, 1] - p[:, 0, 1]) - (p[:, 2, 0] - p[:, 0, 0]) * (p[:, 1, 1] - p[:, 0, 1]))
     l2 = ((p[:, 1] - p[:, 0]) ** 2).sum(1) + ((p[:, 2] - p[:, 1]) ** 2).sum(1) + ((p[:, 0] - p[:, 2]) ** 2).sum(1)
     assert (4 * np.sqrt(3) * a / l2).min() > 0.1
+
+
+BITCONV_CHECK = r"""
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <random>
+#include "bitconv.h"
+static uint32_t fb(float x) { uint32_t u; std::memcpy(&u, &x, 4); return u; }
+static uint64_t db(double x) { uint64_t u; std::memcpy(&u, &x, 8); return u; }
+static float bf(uint32_t u) { float x; std::memcpy(&x, &u, 4); return x; }
+static double bd(uint64_t u) { double x; std::memcpy(&x, &u, 8); return x; }
+static long bad = 0, n = 0;
+static void check_d2f(uint64_t u) {
+    double d = bd(u);
+    uint32_t got = ebbbits::d2f_bits((uint32_t)(u >> 32), (uint32_t)u);
+    n++;
+    if (std::isnan(d)) { if (!std::isnan(bf(got))) bad++; return; }
+    uint32_t want = std::fabs(d) < 0x1p-126 ? (uint32_t)(u >> 32) & 0x80000000u : fb((float)d);
+    if (got != want) { if (bad < 5) std::printf("d2f %016llx got %08x want %08x\n", (unsigned long long)u, got, want); bad++; }
+}
+static void check_f2d(uint32_t f) {
+    float x = bf(f);
+    uint64_t got = ebbbits::f2d_bits(f);
+    n++;
+    if (std::isnan(x)) { if (!std::isnan(bd(got))) bad++; return; }
+    uint64_t want = ((f >> 23) & 0xffu) == 0 ? (uint64_t)(f & 0x80000000u) << 32 : db((double)x);
+    if (got != want) { if (bad < 5) std::printf("f2d %08x got %016llx\n", f, (unsigned long long)got); bad++; }
+}
+int main() {
+    std::mt19937_64 rng(7);
+    for (uint64_t f = 0; f < (1ull << 32); f += 9973) check_f2d((uint32_t)f);
+    const uint32_t fe[] = {0u, 0x80000000u, 1u, 0x807fffffu, 0x00800000u, 0x7f7fffffu, 0xff7fffffu,
+                           0x7f800000u, 0xff800000u, 0x7fc00000u, 0x7f800001u, 0x3f800000u, 0xbf800001u};
+    for (uint32_t f : fe) check_f2d(f);
+    for (int k = 0; k < 4000000; k++) check_d2f(rng());
+    for (int k = 0; k < 4000000; k++) {  // doubles in and near the FP32 range, ties included
+        uint64_t e = 896 + rng() % 260, m = rng() & 0xfffffffffffffull;
+        if (k & 1) m = (m & ~0x1fffffffull) | 0x10000000ull;
+        if (k % 3 == 0) m |= 0x1fffffffull;
+        check_d2f(((rng() & 1) << 63) | (e << 52) | m);
+    }
+    const double de[] = {0.0, -0.0, 1.0, -1.0, 0x1p-126, 0x1p-127, -0x1.fffffffp-127, 0x1.fffffep127,
+                         0x1.ffffffp127, 0x1.fffffefffffffp127, 3.4028235677973366e38, INFINITY, -INFINITY,
+                         NAN, 1e-300, 1e300, 0.1, 1.0 / 3.0};
+    for (double d : de) check_d2f(db(d));
+    std::printf("%ld %ld\n", n, bad);
+    return 0;
+}
+"""
+
+
+def test_integer_pipe_conversions_match_ieee(tmp_path):
+    """The split path's integer-pipe float<->double conversions (csrc/bitconv.h) give
+    the host's IEEE conversions bit for bit: every 9973rd FP32 pattern, 8M doubles
+    (random patterns and values in and near the FP32 range with exact ties), and the
+    edge values; subnormal FP32 results and inputs become signed zeros."""
+    import subprocess
+    src = tmp_path / "bitconv_check.cpp"
+    src.write_text(BITCONV_CHECK)
+    exe = tmp_path / "bitconv_check"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "ebbcfd_gb300", "csrc"), str(src),
+                    "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    n, bad = int(out[-2]), int(out[-1])
+    assert n > 8_000_000 and bad == 0, " ".join(out[:-2])
