@@ -374,7 +374,7 @@ size_t bytes_of(const Dims &D, int32_t precision)
     total += rsz(4 * MJ * Cs) + rsz(8 * NQ);               // face, grad
     total += rsz(4 * (Et + Gt)) + rsz(Et + Gt) + rsz(Ct);  // fl, fs, cdt
     total += sz<double>(8 * (size_t)D.nblk) + sz<DState>(n) + sz<DRecord>(EBB_REC_CAP);
-    total += 3 * sz<int32_t>(Ct) + 3 * rsz(Ct) + (D.any_mms ? rsz(4 * Ct) : 0);
+    total += 4 * sz<int32_t>(Ct) + 3 * rsz(Ct) + (D.any_mms ? rsz(4 * Ct) : 0);
     total += 2 * sz<int32_t>(MJ * Cs) + 3 * rsz(2 * MJ * Cs);
     total += 2 * sz<int32_t>(2 * Et) + rsz(2 * Et) + rsz(Et) + sz<int32_t>(Et);
     total += 4 * sz<int32_t>(Gt) + rsz(2 * Gt) + rsz(Gt) + 4 * rsz(4 * Gt);
@@ -580,6 +580,11 @@ int assemble(ebb_solver *s, std::vector<InstLayout> &Ls, int32_t precision, std:
     M.nedge = up(ar.take<int32_t>(Ct), nedge);
     M.cell_ref = up(ar.take<int32_t>(Ct), cellref);
     s->d_perm = up(ar.take<int32_t>(Ct), s->perm);
+    {
+        std::vector<int32_t> iperm(Ct);
+        for (int64_t i = 0; i < Ct; i++) iperm[s->perm[i]] = (int32_t)i;
+        s->d_iperm = up(ar.take<int32_t>(Ct), iperm);
+    }
     M.g.neg_inv_area = upR(nia);
     M.g.perim = upR(perim);
     M.g.dlen = upR(d);

@@ -147,6 +147,34 @@ __global__ void k_to_double4(const float *__restrict__ src, double *__restrict__
     st4(dst + 4 * i, v);
 }
 
+// State in and out in the caller's cell order.  The reference-order side is read or
+// written in sequence (the device side through the inverse permutation), so when it
+// is a page-locked host buffer the link carries whole contiguous lines.
+__global__ void k_load_state(const double *__restrict__ src, double *__restrict__ q64, float *__restrict__ qs1,
+                             const int32_t *__restrict__ iperm, int64_t n)
+{
+    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    double v[4];
+    ld4(src + 4 * j, v);
+    const size_t i = (size_t)iperm[j];
+    st4(q64 + 4 * i, v);
+    if (qs1) {
+        float f[4] = {(float)v[0], (float)v[1], (float)v[2], (float)v[3]};
+        st4(qs1 + 4 * i, f);
+    }
+}
+
+__global__ void k_store_state(const double *__restrict__ q64, double *__restrict__ dst,
+                              const int32_t *__restrict__ iperm, int64_t n)
+{
+    int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    double v[4];
+    ld4(q64 + 4 * (size_t)iperm[j], v);
+    st4(dst + 4 * j, v);
+}
+
 inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
 }  // namespace
@@ -192,5 +220,19 @@ int launch_to_double4(const float *src, double *dst, int64_t n, void *stream)
 {
     if (n <= 0) return 0;
     k_to_double4<<<nblk(n, 256), 256, 0, (cudaStream_t)stream>>>(src, dst, n);
+    return ret(cudaGetLastError());
+}
+
+int launch_load_state(const double *src, double *q64, float *qs1, const int32_t *iperm, int64_t n, void *stream)
+{
+    if (n <= 0) return 0;
+    k_load_state<<<nblk(n, 256), 256, 0, (cudaStream_t)stream>>>(src, q64, qs1, iperm, n);
+    return ret(cudaGetLastError());
+}
+
+int launch_store_state(const double *q64, double *dst, const int32_t *iperm, int64_t n, void *stream)
+{
+    if (n <= 0) return 0;
+    k_store_state<<<nblk(n, 256), 256, 0, (cudaStream_t)stream>>>(q64, dst, iperm, n);
     return ret(cudaGetLastError());
 }

@@ -151,5 +151,9 @@ int update_blocks(int C);
 int launch_permute4(const double *src, double *dst, const int32_t *idx, int64_t n, int gather, void *stream);
 int launch_to_float4(const double *src, float *dst, int64_t n, void *stream);
 int launch_to_double4(const float *src, double *dst, int64_t n, void *stream);
+// state in reference order (src, possibly page-locked host memory) -> device order
+// q64[iperm[j]] = src[j], plus its FP32 copy when qs1 is given; and back
+int launch_load_state(const double *src, double *q64, float *qs1, const int32_t *iperm, int64_t n, void *stream);
+int launch_store_state(const double *q64, double *dst, const int32_t *iperm, int64_t n, void *stream);
 }
 #endif

@@ -3,6 +3,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <thread>
 
 #include "solver_impl.hpp"
@@ -33,6 +35,59 @@ int fail(ebb_solver *s, int code, const std::string &msg)
         int _r = (x);                                                                          \
         if (_r != 0) return fail(s, EBB_ERR_CUDA, "kernel launch failed");                     \
     } while (0)
+
+// Page-locked buffers from ebb_host_alloc, by base address, with the address the
+// device reads them at.  A state upload from inside one of them is read by the state
+// kernel directly over the host link (in sequence; as fast as a copy engine on GB300,
+// and it saves the staging copy's device pass).  Downloads always go through a
+// staging array and a copy engine: device stores to host memory ran at less than
+// half the copy engine's rate.
+struct HostBuf {
+    size_t bytes;
+    char *dev;
+};
+std::mutex g_host_mu;
+std::map<uintptr_t, HostBuf> g_host;
+
+// device address of [p, p + bytes) when it lies inside one ebb_host_alloc buffer and
+// starts on a 16-byte boundary (the state kernels move a cell as 16-byte vectors);
+// otherwise null, and the caller stages through device memory
+void *host_mapped(const void *p, size_t bytes)
+{
+    std::lock_guard<std::mutex> l(g_host_mu);
+    const uintptr_t a = (uintptr_t)p;
+    auto it = g_host.upper_bound(a);
+    if (it == g_host.begin()) return nullptr;
+    --it;
+    if (a - it->first > it->second.bytes || bytes > it->second.bytes - (a - it->first)) return nullptr;
+    char *d = it->second.dev + (a - it->first);
+    return ((uintptr_t)d & 15u) == 0 ? d : nullptr;
+}
+
+// caller-order state (host) -> device state q64 (and its FP32 copy), cells [c0, c0+n)
+int state_in(ebb_solver *s, const double *q, int64_t c0, int64_t n)
+{
+    const size_t nb = sizeof(double) * 4 * (size_t)n;
+    const double *src = static_cast<const double *>(host_mapped(q, nb));
+    if (!src) {
+        CK(cudaMemcpyAsync(s->d_stage + 4 * c0, q, nb, cudaMemcpyHostToDevice, s->stream));
+        src = s->d_stage + 4 * c0;
+    }
+    float *qs1 = s->precision == EBB_PREC_SPLIT ? reinterpret_cast<float *>(s->A.qs1) : nullptr;
+    CKL(launch_load_state(src, s->A.q64, qs1, s->d_iperm + c0, n, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return EBB_OK;
+}
+
+// device state q64 -> caller-order state (host), cells [c0, c0+n)
+int state_out(ebb_solver *s, double *q, int64_t c0, int64_t n)
+{
+    const size_t nb = sizeof(double) * 4 * (size_t)n;
+    CKL(launch_store_state(s->A.q64, s->d_stage + 4 * c0, s->d_iperm + c0, n, s->stream));
+    CK(cudaMemcpyAsync(q, s->d_stage + 4 * c0, nb, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return EBB_OK;
+}
 
 inline unsigned long long dbits(double v)
 {
@@ -258,10 +313,25 @@ int ebb_set_device(int device)
 int ebb_host_alloc(size_t bytes, void **ptr)
 {
     if (!ptr) return EBB_ERR_ARG;
-    return cudaMallocHost(ptr, bytes) == cudaSuccess ? EBB_OK : EBB_ERR_OOM;
+    if (cudaMallocHost(ptr, bytes) != cudaSuccess) return EBB_ERR_OOM;
+    void *dev = nullptr;
+    if (cudaHostGetDevicePointer(&dev, *ptr, 0) == cudaSuccess && dev) {
+        std::lock_guard<std::mutex> l(g_host_mu);
+        g_host[(uintptr_t)*ptr] = HostBuf{bytes, static_cast<char *>(dev)};
+    } else {
+        cudaGetLastError();  // not device-mapped: state copies stage through device memory
+    }
+    return EBB_OK;
 }
 
-int ebb_host_free(void *ptr) { return cudaFreeHost(ptr) == cudaSuccess ? EBB_OK : EBB_ERR_CUDA; }
+int ebb_host_free(void *ptr)
+{
+    {
+        std::lock_guard<std::mutex> l(g_host_mu);
+        g_host.erase((uintptr_t)ptr);
+    }
+    return cudaFreeHost(ptr) == cudaSuccess ? EBB_OK : EBB_ERR_CUDA;
+}
 
 int ebb_solver_create(const ebb_mesh *mesh, const ebb_config *cfg, int32_t precision, ebb_solver **out, char *err,
                       size_t err_len)
@@ -342,21 +412,13 @@ int ebb_last_error(const ebb_solver *s, int32_t *kind, int64_t *index, char *msg
 int ebb_set_state(ebb_solver *s, const double *q)
 {
     if (!s || !q) return EBB_ERR_ARG;
-    CK(cudaMemcpyAsync(s->d_stage, q, sizeof(double) * 4 * s->C, cudaMemcpyHostToDevice, s->stream));
-    CKL(launch_permute4(s->d_stage, s->A.q64, s->d_perm, s->C, 1, s->stream));
-    if (s->precision == EBB_PREC_SPLIT)
-        CKL(launch_to_float4(s->A.q64, reinterpret_cast<float *>(s->A.qs1), s->C, s->stream));
-    CK(cudaStreamSynchronize(s->stream));
-    return EBB_OK;
+    return state_in(s, q, 0, s->C);
 }
 
 int ebb_get_state(ebb_solver *s, double *q)
 {
     if (!s || !q) return EBB_ERR_ARG;
-    CKL(launch_permute4(s->A.q64, s->d_stage, s->d_perm, s->C, 0, s->stream));
-    CK(cudaMemcpyAsync(q, s->d_stage, sizeof(double) * 4 * s->C, cudaMemcpyDeviceToHost, s->stream));
-    CK(cudaStreamSynchronize(s->stream));
-    return EBB_OK;
+    return state_out(s, q, 0, s->C);
 }
 
 int ebb_get_time(ebb_solver *s, double *t, double *dt, int64_t *iterations)
@@ -648,22 +710,14 @@ int ebb_batch_get_state(ebb_solver *s, int32_t k, double *q)
 {
     if (!s || !q || k < 0 || k >= s->n_inst) return EBB_ERR_ARG;
     const InstMeta &m = s->inst[k];
-    CKL(launch_permute4(s->A.q64 + 4 * m.c0, s->d_stage, s->d_perm + m.c0, m.C, 0, s->stream));
-    CK(cudaMemcpyAsync(q, s->d_stage + 4 * m.c0, sizeof(double) * 4 * m.C, cudaMemcpyDeviceToHost, s->stream));
-    CK(cudaStreamSynchronize(s->stream));
-    return EBB_OK;
+    return state_out(s, q, m.c0, m.C);
 }
 
 int ebb_batch_set_state(ebb_solver *s, int32_t k, const double *q)
 {
     if (!s || !q || k < 0 || k >= s->n_inst) return EBB_ERR_ARG;
     const InstMeta &m = s->inst[k];
-    CK(cudaMemcpyAsync(s->d_stage + 4 * m.c0, q, sizeof(double) * 4 * m.C, cudaMemcpyHostToDevice, s->stream));
-    CKL(launch_permute4(s->d_stage, s->A.q64 + 4 * m.c0, s->d_perm + m.c0, m.C, 1, s->stream));
-    if (s->precision == EBB_PREC_SPLIT)
-        CKL(launch_to_float4(s->A.q64 + 4 * m.c0, reinterpret_cast<float *>(s->A.qs1) + 4 * m.c0, m.C, s->stream));
-    CK(cudaStreamSynchronize(s->stream));
-    return EBB_OK;
+    return state_in(s, q, m.c0, m.C);
 }
 
 int ebb_launch_steps(ebb_solver *s, int64_t n_steps)

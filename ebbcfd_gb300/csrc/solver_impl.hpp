@@ -52,6 +52,7 @@ struct ebb_solver {
     DPhys P{};
     DArrays A{};
     int32_t *d_perm = nullptr;
+    int32_t *d_iperm = nullptr;  // reference cell -> device cell
     double *d_stage = nullptr;  // C x 4 doubles in reference order
     double *d_tmp = nullptr;    // C x 4 doubles in device order (split-path conversions)
     int nred = 0;
