@@ -234,9 +234,7 @@ def run_ours(args, ws, rank, local):
         split = {"value": m32["value"], "unit": "cell-updates/s", "ms_per_step": 1e3 * m32["elapsed"] / m32["steps"],
                  "speedup_vs_fp64": m32["value"] / m64["value"], "roofline": m32["roofline"],
                  # L2 error per component relative to the component's RMS, and the largest
-                 # pointwise error relative to the component's largest magnitude (that one
-                 # sits at the shock, where a sub-cell shift of the captured profile gives
-                 # an O(1) local difference)
+                 # pointwise error relative to the component's largest magnitude
                  "state_l2_err_vs_fp64": [float(x) for x in np.sqrt(((q32 - q64) ** 2).mean(axis=0)
                                                                    / np.maximum((q64 ** 2).mean(axis=0), 1e-300))],
                  "state_max_err_vs_fp64": float((np.abs(q32 - q64).max(axis=0) / scale).max()),
