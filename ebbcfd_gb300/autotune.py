@@ -27,7 +27,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 # per precision form and kernel: candidate minimum blocks per SM, one row per build
-CANDIDATES = {"split": {"cell": [8, 10, 12, 14], "flux": [10, 12, 16, 20], "update": [4, 6, 8, 8]},
+CANDIDATES = {"split": {"cell": [6, 8, 10, 12], "flux": [10, 12, 16, 20], "update": [4, 6, 8, 8]},
               "fp64": {"cell": [1, 5, 6, 8], "flux": [1, 5, 6, 8], "update": [1, 2, 3, 4]}}
 MACRO = {("split", "cell"): "EBB_CELL_MINB_F", ("split", "flux"): "EBB_FLUX_MINB_F",
          ("split", "update"): "EBB_UPD_MINB_F", ("fp64", "cell"): "EBB_CELL_MINB_D",

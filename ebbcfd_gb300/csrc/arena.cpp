@@ -559,6 +559,7 @@ int assemble(ebb_solver *s, std::vector<InstLayout> &Ls, int32_t precision, std:
     M.Cs = (int32_t)Cs;
     M.Eint = (int32_t)Et;
     M.maxJ = MJ;
+    M.uniform = std::all_of(nedge.begin(), nedge.end(), [&](int32_t v) { return v == MJ; }) ? 1 : 0;
     M.n_inst = n;
     M.n_upd_blocks = nblk;
     auto up = [&](auto *dst, const auto &v) {

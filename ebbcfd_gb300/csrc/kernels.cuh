@@ -346,7 +346,7 @@ __device__ __forceinline__ void lp_limit(const DMesh &M, int i, int ne, const T 
     }
 }
 
-template <typename T, int MJ, bool LP>
+template <typename T, int MJ, bool LP, bool UNI>
 __global__ void __launch_bounds__(128, sizeof(T) == 4 ? EBB_CELL_MINB_F : EBB_CELL_MINB_D) k_cell(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, int limit)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -360,7 +360,7 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? EBB_CELL_MINB_F : EBB_CE
     int nbv[MJ];
     typename V2<T>::t gmv[MJ], ndv[MJ], fdv[MJ];
     if (act) {
-        ne = M.nedge[i];
+        ne = UNI ? MJ : M.nedge[i];  // UNI: every cell has MJ edges (all triangles, all quads)
         if (M.cell_inst) inst = M.cell_inst[i];
         if constexpr (sizeof(T) == 4) {
 #pragma unroll
@@ -832,7 +832,7 @@ __device__ __forceinline__ float warp_maxf(float v)
 // FP64 for both precision forms.  FP64 path: qin/qout are double stage states as in
 // integrators.d.  Split path: qin is the FP32 stage input, q64 is updated in FP64 and
 // the next stage input (qout) is its FP32 rounding.
-template <typename T, int ST, int MJ>
+template <typename T, int ST, int MJ, bool UNI>
 __global__ void __launch_bounds__(UPD_THREADS, sizeof(T) == 4 ? EBB_UPD_MINB_F : EBB_UPD_MINB_D) k_update(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, T *qout,
                                                        int dt_update, int need_dt, int final_stage)
 {
@@ -854,7 +854,7 @@ __global__ void __launch_bounds__(UPD_THREADS, sizeof(T) == 4 ? EBB_UPD_MINB_F :
     if (act) {
 #pragma unroll
         for (int j = 0; j < MJ; j++) ev[j] = M.s_edge[(size_t)j * Cs + i];
-        ne = M.nedge[i];
+        ne = UNI ? MJ : M.nedge[i];
     }
     grid_dep_release();
     grid_dep_wait();
@@ -1196,19 +1196,26 @@ int launch_cell_impl(const DMesh &M, const DPhys &P, const DArrays &A, const T *
     cudaStream_t s = (cudaStream_t)stream;
     const bool lp = P.lp && P.limited;
     cudaError_t e;
-#define EBB_CELL(MJ)                                                              \
-    if (lp)                                                                       \
-        e = launch_dep(k_cell<T, MJ, true>, grid, dim3(TB), s, M, P, A, qin, limit); \
-    else                                                                          \
-        e = launch_dep(k_cell<T, MJ, false>, grid, dim3(TB), s, M, P, A, qin, limit);
+#define EBB_CELL_U(MJ, U)                                                                 \
+    if (lp)                                                                               \
+        e = launch_dep(k_cell<T, MJ, true, U>, grid, dim3(TB), s, M, P, A, qin, limit);  \
+    else                                                                                  \
+        e = launch_dep(k_cell<T, MJ, false, U>, grid, dim3(TB), s, M, P, A, qin, limit);
+#define EBB_CELL(MJ)           \
+    if (M.uniform) {           \
+        EBB_CELL_U(MJ, true)   \
+    } else {                   \
+        EBB_CELL_U(MJ, false)  \
+    }
     if (M.maxJ <= 3) {
         EBB_CELL(3)
     } else if (M.maxJ == 4) {
         EBB_CELL(4)
-    } else {
-        EBB_CELL(6)
+    } else {  // meshes of hexagons only are not specialised
+        EBB_CELL_U(6, false)
     }
 #undef EBB_CELL
+#undef EBB_CELL_U
     return ret(e);
 }
 
@@ -1228,16 +1235,20 @@ int launch_update_impl(const DMesh &M, const DPhys &P, const DArrays &A, int sta
     if (grid.x == 0) return 0;
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = cudaSuccess;
-#define EBB_UPD_MJ(S, MJ) \
-    e = launch_dep(k_update<T, S, MJ>, grid, dim3(UPD_THREADS), s, M, P, A, qin, qout, dt_update, need_dt, final_stage)
-#define EBB_UPD(S)                  \
-    case S:                         \
-        if (M.maxJ <= 3)            \
-            EBB_UPD_MJ(S, 3);       \
-        else if (M.maxJ == 4)       \
-            EBB_UPD_MJ(S, 4);       \
-        else                        \
-            EBB_UPD_MJ(S, 6);       \
+#define EBB_UPD_MJ(S, MJ)                                                                                         \
+    e = M.uniform ? launch_dep(k_update<T, S, MJ, true>, grid, dim3(UPD_THREADS), s, M, P, A, qin, qout, dt_update,  \
+                               need_dt, final_stage)                                                                 \
+                  : launch_dep(k_update<T, S, MJ, false>, grid, dim3(UPD_THREADS), s, M, P, A, qin, qout, dt_update, \
+                               need_dt, final_stage)
+#define EBB_UPD(S)                                                                                                 \
+    case S:                                                                                                        \
+        if (M.maxJ <= 3)                                                                                           \
+            EBB_UPD_MJ(S, 3);                                                                                      \
+        else if (M.maxJ == 4)                                                                                      \
+            EBB_UPD_MJ(S, 4);                                                                                      \
+        else                                                                                                       \
+            e = launch_dep(k_update<T, S, 6, false>, grid, dim3(UPD_THREADS), s, M, P, A, qin, qout, dt_update,    \
+                           need_dt, final_stage);                                                                  \
         break;
     switch (stage) {
         EBB_UPD(ST_RESID)

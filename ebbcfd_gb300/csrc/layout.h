@@ -32,6 +32,7 @@ struct DGeo {
 
 struct DMesh {
     int32_t C, G, Cs, Eint, maxJ;
+    int32_t uniform;                   // every interior cell has exactly maxJ edges
     const int32_t *nedge;
     const int32_t *s_nbr, *s_edge;
     const int32_t *e_slot, *e_cell;    // int2 per interior edge
