@@ -440,9 +440,9 @@ def run_plate(args):
     return out
 
 
-def bump_json(mach, cfl=0.3, integrator="RK2_TVD"):
+def bump_json(mach, cfl=0.3, integrator="RK2_TVD", flux="roeFlux"):
     q = [mach, 0, 1, 1]
-    return json.dumps({"mesh": "bump.msh", "dt": 1e-4, "tEnd": 1e9, "flux": "roeFlux", "saveIter": -1,
+    return json.dumps({"mesh": "bump.msh", "dt": 1e-4, "tEnd": 1e9, "flux": flux, "saveIter": -1,
                        "plotIter": -1, "forceBoundary": "Wall", "integrator": integrator, "limited": True, "CFL": cfl,
                        "initialConditions": q,
                        "boudaryConditions": [{"tag": "Inflow", "type": "fullState", "q": q},
@@ -585,7 +585,7 @@ def run_serve(args):
     # the served stream names no integrator: RK2 with multistage limiting, which stays
     # bounded where the reference's TVD-RK2 (second stage always unlimited) lets FP32
     # rounding grow into a NaN on some meshes
-    cfgs = [E.load_config(bump_json(float(m), integrator=args.serve_integrator) if k == "bump"
+    cfgs = [E.load_config(bump_json(float(m), integrator=args.serve_integrator, flux=args.serve_flux) if k == "bump"
                           else cylinder_json(float(r), integrator=args.serve_integrator))
             for k, m, r in zip(kinds, machs, res)]
     L = _lib.load()
@@ -620,7 +620,8 @@ def run_serve(args):
     # sequential plain FP64: per-step device time alone x steps run
     per = seq_ms_per_step(L, E, meshes, cfgs, "fp64", args.seq_steps, 3)
     seq_s = float(sum(per[k] * iters[k] for k in range(R)) / 1e3)
-    return {"workload": "served-bump70-cyl30-split", "integrator": args.serve_integrator, "requests": R,
+    return {"workload": "served-bump70-cyl30-split", "integrator": args.serve_integrator,
+            "bump_flux": args.serve_flux, "requests": R,
             "arrival_rate_per_s": 40.0,
             "cells_range": [int(cells.min()), int(cells.max())], "cells_total": int(sum(m.n_cells for m in meshes)),
             "step_cap": cap, "resid_drop": 1e-8, "wall_s": wall, "solves_per_s": R / wall,
@@ -686,6 +687,7 @@ def main():
     ap.add_argument("--max-cells", type=float, default=2e6)
     ap.add_argument("--step-cap", type=int, default=50000)
     ap.add_argument("--serve-integrator", default="RK2", choices=["Euler", "RK2", "RK2_TVD", "RK4"])
+    ap.add_argument("--serve-flux", default="roeFlux", choices=["roeFlux", "rusanovFlux"])
     args = ap.parse_args()
     args.steps_given = "--steps" in sys.argv
     args.cells_given = "--cells" in sys.argv

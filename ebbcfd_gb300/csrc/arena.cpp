@@ -376,6 +376,7 @@ size_t bytes_of(const Dims &D, int32_t precision)
     total += sz<double>(8 * (size_t)D.nblk) + sz<DState>(n) + sz<DRecord>(EBB_REC_CAP);
     total += 4 * sz<int32_t>(Ct) + 3 * rsz(Ct) + (D.any_mms ? rsz(4 * Ct) : 0);
     total += 2 * sz<int32_t>(MJ * Cs) + 3 * rsz(2 * MJ * Cs);
+    total += split ? rsz(2 * MJ * Cs) + rsz(MJ * Cs) : 0;  // per-slot edge normal and length
     total += 2 * sz<int32_t>(2 * Et) + rsz(2 * Et) + rsz(Et) + sz<int32_t>(Et);
     total += 4 * sz<int32_t>(Gt) + rsz(2 * Gt) + rsz(Gt) + 4 * rsz(4 * Gt);
     total += sz<int32_t>(D.nforce + 1) + sz<int32_t>(n + 1);
@@ -599,6 +600,22 @@ int assemble(ebb_solver *s, std::vector<InstLayout> &Ls, int32_t precision, std:
     M.e_cell = up(ar.take<int32_t>(2 * Et), ecell);
     M.g.e_n = upR(en);
     M.g.e_len = upR(elen);
+    if (split) {  // per-slot copies for the split update's freestream correction
+        std::vector<double> sen(2 * MJ * Cs, 0.0), selen(MJ * Cs, 0.0);
+        for (int64_t i = 0; i < Ct; i++)
+            for (int j = 0; j < nedge[i]; j++) {
+                const int64_t gs = (int64_t)j * Cs + i;
+                const int64_t f = sedge[gs] & 0x7fffffff;
+                const bool in = f < Et;
+                sen[2 * gs] = in ? en[2 * f] : bn[2 * (f - Et)];
+                sen[2 * gs + 1] = in ? en[2 * f + 1] : bn[2 * (f - Et) + 1];
+                selen[gs] = in ? elen[f] : blen[f - Et];
+            }
+        M.g.s_en = upR(sen);
+        M.g.s_elen = upR(selen);
+    } else {
+        M.g.s_en = M.g.s_elen = nullptr;
+    }
     M.e_ref = up(ar.take<int32_t>(Et), eref);
     M.b_cell = up(ar.take<int32_t>(Gt), bcell);
     M.b_slot = up(ar.take<int32_t>(Gt), bslot);

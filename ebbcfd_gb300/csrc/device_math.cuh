@@ -61,16 +61,40 @@ __device__ __forceinline__ bool pressure_negative(const double q[4])
 }
 __device__ __forceinline__ bool pressure_negative(const float q[4]) { return pressure(q) < 0; }
 
-// source/flux.d:19-24
+// source/flux.d:19-24.  Single precision rounds every operation on its own (no
+// multiply-add contraction): the flux kernel's value for two equal face states and the
+// update kernel's freestream correction (k_update) then agree bit for bit wherever
+// they are evaluated.
 template <typename T>
 __device__ __forceinline__ void convective_flux(T p, T u, T v, T rho, T e, T nx, T ny, T out[4])
 {
-    T f0 = rho * u, f1 = p + rho * (u * u), f2 = rho * u * v, f3 = u * (p + e);
-    T h0 = rho * v, h1 = rho * u * v, h2 = p + rho * (v * v), h3 = v * (p + e);
-    out[0] = f0 * nx + h0 * ny;
-    out[1] = f1 * nx + h1 * ny;
-    out[2] = f2 * nx + h2 * ny;
-    out[3] = f3 * nx + h3 * ny;
+    if constexpr (sizeof(T) == 4) {
+        const float ru = __fmul_rn(rho, u), rv = __fmul_rn(rho, v), ruv = __fmul_rn(ru, v), pe = __fadd_rn(p, e);
+        const float f1 = __fadd_rn(p, __fmul_rn(rho, __fmul_rn(u, u))), h2 = __fadd_rn(p, __fmul_rn(rho, __fmul_rn(v, v)));
+        const float f3 = __fmul_rn(u, pe), h3 = __fmul_rn(v, pe);
+        out[0] = __fadd_rn(__fmul_rn(ru, nx), __fmul_rn(rv, ny));
+        out[1] = __fadd_rn(__fmul_rn(f1, nx), __fmul_rn(ruv, ny));
+        out[2] = __fadd_rn(__fmul_rn(ruv, nx), __fmul_rn(h2, ny));
+        out[3] = __fadd_rn(__fmul_rn(f3, nx), __fmul_rn(h3, ny));
+    } else {
+        T f0 = rho * u, f1 = p + rho * (u * u), f2 = rho * u * v, f3 = u * (p + e);
+        T h0 = rho * v, h1 = rho * u * v, h2 = p + rho * (v * v), h3 = v * (p + e);
+        out[0] = f0 * nx + h0 * ny;
+        out[1] = f1 * nx + h1 * ny;
+        out[2] = f2 * nx + h2 * ny;
+        out[3] = f3 * nx + h3 * ny;
+    }
+}
+
+// gm1 (e - 0.5 rho (u^2 + v^2)), the pressure of source/flux.d's flux functions;
+// single precision without contraction, as convective_flux
+template <typename T> __device__ __forceinline__ T pressure_of(T rho, T u, T v, T e)
+{
+    if constexpr (sizeof(T) == 4)
+        return __fmul_rn(K<float>::gm1,
+                         __fsub_rn(e, __fmul_rn(__fmul_rn(0.5f, rho), __fadd_rn(__fmul_rn(u, u), __fmul_rn(v, v)))));
+    else
+        return K<T>::gm1 * (e - T(0.5) * rho * (u * u + v * v));
 }
 
 template <typename T> __device__ __forceinline__ T entropy_fix(T lam, T eps)
@@ -95,11 +119,11 @@ __device__ __forceinline__ void roe_flux(const T qL[4], const T qR[4], T nx, T n
     const T gm1 = K<T>::gm1;
     T rhoL = qL[0], uL = qL[1] / rhoL, vL = qL[2] / rhoL;
     T rvL0 = rhoL * uL, rvL1 = rhoL * vL;
-    T pL = gm1 * (qL[3] - T(0.5) * rhoL * (uL * uL + vL * vL));
+    T pL = pressure_of(rhoL, uL, vL, qL[3]);
     T hL = (qL[3] + pL) / rhoL;
     T rhoR = qR[0], uR = qR[1] / rhoR, vR = qR[2] / rhoR;
     T rvR0 = rhoR * uR, rvR1 = rhoR * vR;
-    T pR = gm1 * (qR[3] - T(0.5) * rhoR * (uR * uR + vR * vR));
+    T pR = pressure_of(rhoR, uR, vR, qR[3]);
     T hR = (qR[3] + pR) / rhoR;
 
     T di = dsqrt(rhoR / rhoL);
@@ -164,11 +188,10 @@ __device__ __forceinline__ void rusanov_flux(const T qL[4], const T qR[4], T nx,
             return;
         }
     }
-    const T gm1 = K<T>::gm1;
     T rhoL = qL[0], uL = qL[1] / rhoL, vL = qL[2] / rhoL;
-    T pL = gm1 * (qL[3] - T(0.5) * rhoL * (uL * uL + vL * vL));
+    T pL = pressure_of(rhoL, uL, vL, qL[3]);
     T rhoR = qR[0], uR = qR[1] / rhoR, vR = qR[2] / rhoR;
-    T pR = gm1 * (qR[3] - T(0.5) * rhoR * (uR * uR + vR * vR));
+    T pR = pressure_of(rhoR, uR, vR, qR[3]);
     T rho = dsqrt(rhoL * rhoR);
     T sL = dsqrt(rhoL), sR = dsqrt(rhoR);
     T vel0 = (sL * uL + sR * uR) / (sL + sR);
@@ -208,11 +231,11 @@ __device__ __forceinline__ void rusanov_flux_full(const T qL[4], const T qR[4], 
     const T gm1 = K<T>::gm1;
     T rhoL = qL[0], uL = qL[1] / rhoL, vL = qL[2] / rhoL;
     T rvL0 = rhoL * uL, rvL1 = rhoL * vL;
-    T pL = gm1 * (qL[3] - T(0.5) * rhoL * (uL * uL + vL * vL));
+    T pL = pressure_of(rhoL, uL, vL, qL[3]);
     T hL = (qL[3] + pL) / rhoL;
     T rhoR = qR[0], uR = qR[1] / rhoR, vR = qR[2] / rhoR;
     T rvR0 = rhoR * uR, rvR1 = rhoR * vR;
-    T pR = gm1 * (qR[3] - T(0.5) * rhoR * (uR * uR + vR * vR));
+    T pR = pressure_of(rhoR, uR, vR, qR[3]);
     T hR = (qR[3] + pR) / rhoR;
 
     T rho = dsqrt(rhoL * rhoR);

@@ -851,10 +851,19 @@ __global__ void __launch_bounds__(UPD_THREADS, sizeof(T) == 4 ? EBB_UPD_MINB_F :
     // read-only mesh data before the wait for the previous kernel: every edge row is
     // loaded whatever the cell's edge count (rows past it hold 0)
     int ev[MJ], ne = 0;
+    typename V2<T>::t sn[MJ];  // split path: the slots' edge normals and lengths
+    T sl[MJ];
     if (act) {
 #pragma unroll
         for (int j = 0; j < MJ; j++) ev[j] = M.s_edge[(size_t)j * Cs + i];
         ne = UNI ? MJ : M.nedge[i];
+        if constexpr (SPLIT) {
+#pragma unroll
+            for (int j = 0; j < MJ; j++) {
+                sn[j] = ld2<T>(M.g.s_en, (size_t)j * Cs + i);
+                sl[j] = ld1<T>(M.g.s_elen, (size_t)j * Cs + i);
+            }
+        }
     }
     grid_dep_release();
     grid_dep_wait();
@@ -892,6 +901,42 @@ __global__ void __launch_bounds__(UPD_THREADS, sizeof(T) == 4 ? EBB_UPD_MINB_F :
                 }
                 sAve += fe[j];
             }
+        }
+        if constexpr (SPLIT) {
+            // Freestream preservation.  Subtract the same edge sum of the cell's own
+            // physical flux, sum_j m_j len_j F(q_i).n_j = F(q_i) . sum_j m_j len_j n_j,
+            // which is zero but for the rounding of the FP32 edge terms.  Where the
+            // cell and its neighbours hold one state (face states equal to it, the flux
+            // of two equal states equal to the physical flux, computed without
+            // contraction in both kernels) both sums are the same bits and the residual
+            // is exactly zero, as in FP64; otherwise the correction is of the size of
+            // the FP32 rounding.  Without it a uniform region takes FP32-rounding-size
+            // increments every step, which seed the locally unstable modes the scheme
+            // has on some meshes (a plain FP64 run with 1e-7 noise added each step
+            // fails at the same edge as the split run).
+            T qc[4];
+            ld4(qin + 4 * (size_t)i, qc);
+            const T uc = qc[1] / qc[0], vc = qc[2] / qc[0];
+            const T pc = pressure_of(qc[0], uc, vc, qc[3]);
+            T c[4] = {T(0.0), T(0.0), T(0.0), T(0.0)};
+#pragma unroll
+            for (int j = 0; j < MJ; j++) {
+                if (j < ne) {
+                    const T len = sl[j];
+                    T F[4];
+                    convective_flux(pc, uc, vc, qc[0], qc[3], sn[j].x, sn[j].y, F);
+                    // len F rounded on its own, as k_flux stores it (no contraction)
+                    if (ev[j] < 0) {
+#pragma unroll
+                        for (int k = 0; k < 4; k++) c[k] = __fadd_rn(c[k], -__fmul_rn(len, F[k]));
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < 4; k++) c[k] = __fadd_rn(c[k], __fmul_rn(len, F[k]));
+                    }
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 4; k++) r[k] = r[k] - c[k];
         }
         T *cdt = reinterpret_cast<T *>(A.cdt);
         if (need_dt || (P.local_ts && dt_update)) {

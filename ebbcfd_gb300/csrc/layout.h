@@ -26,6 +26,8 @@ struct DGeo {
     const void *neg_inv_area, *perim, *dlen;     // T per cell
     const void *src;                             // T[4] per cell or null
     const void *e_n, *e_len;                     // T[2], T per interior edge
+    const void *s_en, *s_elen;                   // split path: T[2], T per slot, a copy of
+                                                 // the slot's edge normal and length
     const void *b_n, *b_len;                     // T[2], T per boundary edge
     const void *b_refl, *b_data, *b_dq, *b_dmid; // T[4] per boundary edge
 };

@@ -11,7 +11,7 @@ tags 1..N in PhysicalNames order, triangles type 2, quads type 3.
   finer toward the ramp.  Tags: Inflow (x=0), Top (y=1), Symmetry (y=0, x<0.5), Ramp,
   Outflow (x=3).
 * ``bump_channel``: [0,3]x[0,1] with a bump y = h sin^2(pi (x-1)) on 1<=x<=2;
-  Delaunay triangles.  Tags: Inflow, Outflow, Wall.
+  Delaunay triangles of Poisson-disk points.  Tags: Inflow, Outflow, Wall.
 * ``flat_plate``: [-0.5,2]x[0,0.5]; anisotropic quads in a wall layer (first cell
   1e-4, growth 1.05) and Delaunay triangles above.  Tags: Inflow, Top, Outflow,
   Symmetry (y=0, x<0), Wall (y=0, x>=0).
@@ -267,7 +267,8 @@ def wedge(n_cells=1_000_000, seed=0, angle_deg=15.0, ramp_x=0.5):
 
 
 def bump_channel(n_cells=20000, h=0.05, seed=0):
-    rng = np.random.default_rng(seed)
+    """Poisson-disk interior points (minimum triangle angle ~17 degrees and up; a
+    jittered grid, the earlier choice, left angles down to ~10 degrees)."""
 
     def floor_y(x):
         x = np.asarray(x, float)
@@ -275,7 +276,7 @@ def bump_channel(n_cells=20000, h=0.05, seed=0):
 
     area = 3.0 - 0.5 * h
     hc = math.sqrt(area / (n_cells / 2.0))
-    hfun = lambda x, y: np.full(np.shape(x), hc) if np.ndim(x) else hc
+    hfun = lambda x, y: np.full(np.shape(x), hc)  # noqa: E731
     xs = np.arange(0, 3 + 1e-12, hc)
     xs[-1] = 3.0
     bottom = np.column_stack([xs, floor_y(xs)])
@@ -288,7 +289,13 @@ def bump_channel(n_cells=20000, h=0.05, seed=0):
     def inside(x, y, margin):
         return (x > margin) & (x < 3 - margin) & (y < 1 - margin) & (y - floor_y(x) > margin)
 
-    ip = _interior_points(rng, 0, 3, 0, 1, lambda x, y: np.full(np.shape(x), hc), inside, hc)
+    rho = 0.71  # the triangle count goes as rho^-1.74; a second pass corrects rho when off by > 2%
+    for _ in range(2):
+        ip = _poisson_points(np.random.default_rng(seed), 0, 3, 0, 1, hfun, inside, hc, rho)
+        ratio = (2 * len(ip) + len(bpts)) / n_cells
+        if abs(ratio - 1) < 0.02:
+            break
+        rho *= ratio ** (1 / 1.74)
     nodes = np.vstack([bpts, ip])
     tri = Delaunay(nodes).simplices.astype(np.int64)
     # the convex hull also covers the region under the bump: drop those triangles
