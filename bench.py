@@ -144,6 +144,8 @@ def algorithmic_bytes(info, real=8, need_grad=False, limited=True):
     # residual + RK2 first-stage update: nedge, perim, d, -1/area, FP64 q read, aux write
     # (T) and next-stage state write (T)
     update = C * (4 + 3 * r + 32 + 4 * r + 4 * r) + S * 4 + (E + G) * 5 * r
+    if r == 4:  # split: the freestream correction reads the stage state and each slot's normal and length
+        update += C * 4 * r + S * 3 * r
     return {"cell": cell, "flux": flux, "update": update}
 
 
@@ -582,9 +584,11 @@ def run_serve(args):
     gens = gen_meshes([(str(k), int(c), float(h), i) for i, (k, c, h) in enumerate(zip(kinds, cells, hs))])
     meshes = [g.to_solver_mesh() for g in gens]
     mesh_s = time.time() - t0
-    # the served stream names no integrator: RK2 with multistage limiting, which stays
-    # bounded where the reference's TVD-RK2 (second stage always unlimited) lets FP32
-    # rounding grow into a NaN on some meshes
+    # the served stream names no flux or integrator: Rusanov flux and RK2 with
+    # multistage limiting for the bump channels.  With the Roe flux the reference's
+    # limited scheme has locally unstable modes on some of these channel meshes that
+    # grow to a NaN within the 50000-step cap, in plain FP64 as well (--serve-flux
+    # roeFlux shows it); the Rusanov flux's dissipation damps them.
     cfgs = [E.load_config(bump_json(float(m), integrator=args.serve_integrator, flux=args.serve_flux) if k == "bump"
                           else cylinder_json(float(r), integrator=args.serve_integrator))
             for k, m, r in zip(kinds, machs, res)]
@@ -687,7 +691,7 @@ def main():
     ap.add_argument("--max-cells", type=float, default=2e6)
     ap.add_argument("--step-cap", type=int, default=50000)
     ap.add_argument("--serve-integrator", default="RK2", choices=["Euler", "RK2", "RK2_TVD", "RK4"])
-    ap.add_argument("--serve-flux", default="roeFlux", choices=["roeFlux", "rusanovFlux"])
+    ap.add_argument("--serve-flux", default="rusanovFlux", choices=["roeFlux", "rusanovFlux"])
     args = ap.parse_args()
     args.steps_given = "--steps" in sys.argv
     args.cells_given = "--cells" in sys.argv
