@@ -150,7 +150,11 @@ int ebb_struct_sizes(size_t *config, size_t *mesh_info, size_t *step_record);
 int ebb_device_count(int *n_devices);
 /* Select the device later solver handles are created on (one GPU per process). */
 int ebb_set_device(int device);
-/* Page-locked host buffers for fast state copies (cudaMallocHost / cudaFreeHost). */
+/* Page-locked host buffers for fast state copies (cudaMallocHost / cudaFreeHost).  A
+   state upload (ebb_set_state, ebb_batch_set_state) whose array starts on a 16-byte
+   boundary inside such a buffer is read by the device directly, with no staging copy;
+   any other host array is staged through device memory.  The buffer must stay
+   allocated for the duration of the call only. */
 int ebb_host_alloc(size_t bytes, void **ptr);
 int ebb_host_free(void *ptr);
 
