@@ -504,15 +504,16 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? EBB_CELL_MINB_F : EBB_CE
                     nd = ndv[j];
                 else
                     nd = ld2<T>(M.g.s_nd, (size_t)j * Cs + i);
+                // every pair's quotient is formed and selected (no divergent branch; the
+                // FP32 division is a reciprocal and a multiply): pairs in bounds leave the
+                // limiter unchanged, as s = 1 does in solve.d:360-402
 #pragma unroll
                 for (int k = 0; k < 4; k++) {
-                    T s = T(1.0);
-                    T qE = qi[k] + (g[k][0] * nd.x + g[k][1] * nd.y);
-                    if (qE < mn[k])
-                        s = (mn[k] - qi[k]) / (g[k][0] * nd.x + g[k][1] * nd.y);
-                    else if (qE > mx[k])
-                        s = (mx[k] - qi[k]) / (g[k][0] * nd.x + g[k][1] * nd.y);
-                    lim0[k] = fmin(lim0[k], s);
+                    const T dd = g[k][0] * nd.x + g[k][1] * nd.y;
+                    const T qE = qi[k] + dd;
+                    const bool lo = qE < mn[k], hi = qE > mx[k];
+                    const T s = ((lo ? mn[k] : mx[k]) - qi[k]) / dd;
+                    lim0[k] = (lo || hi) ? fmin(lim0[k], s) : lim0[k];
                     lim1[k] = lim0[k];
                 }
             }
