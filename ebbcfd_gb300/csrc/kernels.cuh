@@ -1136,38 +1136,45 @@ __global__ void __launch_bounds__(UPD_THREADS, sizeof(T) == 4 ? EBB_UPD_MINB_F :
     if (bad) flag_error(st, 3, ERR_NAN_CELL, (unsigned)M.cell_ref[i]);
     // block reductions: dt (min), Rmax (max), RMS partials (sum) in a fixed tree
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (SPLIT) {  // 32-lane partials in FP32, block and grid accumulation in FP64
-        fdtc = warp_minf(fdtc);
-        frm = warp_maxf(frm);
+    if (SPLIT) {
+        // The whole block in FP32 (an FP64 instruction costs a warp the same with one
+        // lane active as with 32), one conversion per block value; the grid-wide
+        // accumulation of the block partials is FP64.  Every thread's values go to
+        // shared memory and one warp reduces each column (lane l takes rows l, l+32,
+        // ..., then a shuffle tree): 10 values cost a warp ~60 instructions instead of
+        // ten 5-level shuffle trees.  Column 1 holds -Rmax so that columns 0 and 1 are
+        // both minima.  Fixed order.
+        constexpr int WF = 11;  // row stride in floats: conflict-free column reads
+        __shared__ float shf[UPD_THREADS * WF];
+        __shared__ float partf[10];
+        const int t = threadIdx.x;
+        const int ncol = final_stage ? 10 : 2;
+        shf[t * WF + 0] = fdtc;
+        shf[t * WF + 1] = -frm;
         if (final_stage) {
 #pragma unroll
             for (int k = 0; k < 4; k++) {
-                fss[k] = warp_sumf(fss[k]);
-                fvs[k] = warp_sumf(fvs[k]);
-            }
-        }
-        // whole block in FP32 (an FP64 instruction costs a warp the same with one lane
-        // active as with 32), one conversion per block; the grid-wide accumulation of
-        // the block partials is FP64
-        __shared__ float shf[UPD_THREADS / 32][10];
-        if (lane == 0) {
-            shf[w][0] = fdtc;
-            shf[w][1] = frm;
-            for (int k = 0; k < 4; k++) {
-                shf[w][2 + k] = fss[k];
-                shf[w][6 + k] = fvs[k];
+                shf[t * WF + 2 + k] = fss[k];
+                shf[t * WF + 6 + k] = fvs[k];
             }
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            float a = shf[0][0], b = shf[0][1];
-            float s8[8];
-            for (int k = 0; k < 8; k++) s8[k] = shf[0][2 + k];
-            for (int ww = 1; ww < UPD_THREADS / 32; ww++) {
-                a = fminf(a, shf[ww][0]);
-                b = fmaxf(b, shf[ww][1]);
-                for (int k = 0; k < 8; k++) s8[k] = s8[k] + shf[ww][2 + k];
+        for (int c = w; c < ncol; c += UPD_THREADS / 32) {
+            float a = shf[lane * WF + c];
+            if (c < 2) {
+#pragma unroll
+                for (int r = 1; r < UPD_THREADS / 32; r++) a = fminf(a, shf[(lane + 32 * r) * WF + c]);
+                a = warp_minf(a);
+            } else {
+#pragma unroll
+                for (int r = 1; r < UPD_THREADS / 32; r++) a = a + shf[(lane + 32 * r) * WF + c];
+                a = warp_sumf(a);
             }
+            if (lane == 0) partf[c] = a;
+        }
+        __syncthreads();
+        if (t == 0) {
+            const float a = partf[0], b = -partf[1];
             if (need_dt && a == a) {
                 const double ad = (double)a;
                 atomicMin(&st->newdt_bits, (unsigned long long)__double_as_longlong(ad));
@@ -1177,7 +1184,7 @@ __global__ void __launch_bounds__(UPD_THREADS, sizeof(T) == 4 ? EBB_UPD_MINB_F :
                 atomicMax(&st->rmax_bits, (unsigned long long)__double_as_longlong(bd));
             }
             if (final_stage)
-                for (int k = 0; k < 8; k++) A.red[8 * (size_t)blockIdx.x + k] = (double)s8[k];
+                for (int k = 0; k < 8; k++) A.red[8 * (size_t)blockIdx.x + k] = (double)partf[2 + k];
         }
         return;
     } else if constexpr (!SPLIT) {
