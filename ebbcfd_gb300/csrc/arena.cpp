@@ -373,7 +373,6 @@ size_t bytes_of(const Dims &D, int32_t precision)
     total += 2 * rsz(4 * NQ);                              // qs, aux
     total += rsz(4 * MJ * Cs) + rsz(8 * NQ);               // face, grad
     total += rsz(4 * (Et + Gt)) + rsz(Et + Gt) + rsz(Ct);  // fl, fs, cdt
-    total += split ? sz<uint8_t>(Ct) : 0;                   // flat
     total += sz<double>(8 * (size_t)D.nblk) + sz<DState>(n) + sz<DRecord>(EBB_REC_CAP);
     total += 4 * sz<int32_t>(Ct) + 3 * rsz(Ct) + (D.any_mms ? rsz(4 * Ct) : 0);
     total += 2 * sz<int32_t>(MJ * Cs) + 3 * rsz(2 * MJ * Cs);
@@ -550,7 +549,6 @@ int assemble(ebb_solver *s, std::vector<InstLayout> &Ls, int32_t precision, std:
     A.fl = takeR(4 * (Et + Gt));
     A.fs = takeR(Et + Gt);
     A.cdt = takeR(Ct);
-    A.flat = split ? ar.take<uint8_t>(Ct) : nullptr;
     A.red = ar.take<double>(8 * (size_t)nblk);
     A.st = ar.take<DState>(n);
     A.rec = ar.take<DRecord>(EBB_REC_CAP);

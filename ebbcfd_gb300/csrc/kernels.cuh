@@ -397,7 +397,6 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? EBB_CELL_MINB_F : EBB_CE
         for (int j = 0; j < MJ; j++) nbv[j] = (j < ne) ? nbv[j] : i;
 #pragma unroll
         for (int j = 0; j < MJ; j++) ld4(qin + 4 * (size_t)(nbv[j] < M.C ? nbv[j] : i), qv[j]);
-        bool flat = true;  // every neighbour state equal to the cell's own
 #pragma unroll
         for (int j = 0; j < MJ; j++) {
             if (j < ne) {
@@ -405,8 +404,6 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? EBB_CELL_MINB_F : EBB_CE
                     ghost_state<T>(M, P, st, nbv[j] - M.C, qi, qv[j]);
                     st4(qghost + 4 * (size_t)nbv[j], qv[j]);
                 }
-#pragma unroll
-                for (int k = 0; k < 4; k++) flat = flat && qv[j][k] == qi[k];
                 if (second) {
 #pragma unroll
                     for (int k = 0; k < 4; k++) {
@@ -419,7 +416,6 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? EBB_CELL_MINB_F : EBB_CE
                 }
             }
         }
-        A.flat[i] = flat ? 1 : 0;  // the update's freestream correction runs where this is set
     } else {
 #pragma unroll
     for (int j = 0; j < MJ; j++) {
@@ -908,9 +904,6 @@ __global__ void __launch_bounds__(UPD_THREADS, sizeof(T) == 4 ? EBB_UPD_MINB_F :
             }
         }
         if constexpr (SPLIT) {
-          T qc[4];  // loaded with the flag, not behind it
-          ld4(qin + 4 * (size_t)i, qc);
-          if (A.flat[i]) {
             // Freestream preservation.  Subtract the same edge sum of the cell's own
             // physical flux, sum_j m_j len_j F(q_i).n_j = F(q_i) . sum_j m_j len_j n_j,
             // which is zero but for the rounding of the FP32 edge terms.  Where the
@@ -921,11 +914,13 @@ __global__ void __launch_bounds__(UPD_THREADS, sizeof(T) == 4 ? EBB_UPD_MINB_F :
             // the FP32 rounding.  Without it a uniform region takes FP32-rounding-size
             // increments every step, which seed the locally unstable modes the scheme
             // has on some meshes (a plain FP64 run with 1e-7 noise added each step
-            // fails at the same edge as the split run).  Only cells whose neighbour
-            // states all equal their own (k_cell sets A.flat) can have an exactly zero
-            // residual, so only they are corrected; elsewhere the rounding of the edge
-            // terms is one FP32 error among others (correcting there as well doubled
-            // the split path's L2 difference from FP64 on the 1M wedge).
+            // fails at the same edge as the split run).  It runs on every cell: limited
+            // to cells whose neighbours hold bitwise their state, 13 of 512 batch
+            // instances failed instead of 6 (nearly uniform cells then take the full
+            // edge-term rounding); limited to neighbours within 1e-3, the failures and
+            // the accuracy were those of the ungated form, at a higher cost.
+            T qc[4];
+            ld4(qin + 4 * (size_t)i, qc);
             const T uc = qc[1] / qc[0], vc = qc[2] / qc[0];
             const T pc = pressure_of(qc[0], uc, vc, qc[3]);
             T c[4] = {T(0.0), T(0.0), T(0.0), T(0.0)};
@@ -947,7 +942,6 @@ __global__ void __launch_bounds__(UPD_THREADS, sizeof(T) == 4 ? EBB_UPD_MINB_F :
             }
 #pragma unroll
             for (int k = 0; k < 4; k++) r[k] = r[k] - c[k];
-          }
         }
         T *cdt = reinterpret_cast<T *>(A.cdt);
         if (need_dt || (P.local_ts && dt_update)) {

@@ -108,7 +108,6 @@ struct DArrays {
     void *aux;            // k1 / R1 / RK4 accumulator in T
     void *face, *grad, *fl, *fs, *cdt, *R;
     void *lim;            // T[8] per cell (lim[k][0], lim[k][1]) when exported, else null
-    uint8_t *flat;        // split path: 1 when a cell's neighbour states all equal its own
     double *red;          // per-block partial sums (8 per block)
     DState *st;
     DRecord *rec;
