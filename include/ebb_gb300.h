@@ -359,7 +359,7 @@ int ebb_flux_noalloc(int32_t kind, int64_t n, const double *qL, const double *qR
 
 /* ---- files ---------------------------------------------------------------- */
 /* .esln v2 of the resident state with the header time t and step dt (saveSolution
-   takes them as arguments: the driver saves before advancing t). */
+   takes them as arguments: the time loop of app/solver.d saves before advancing t). */
 int ebb_save_solution(ebb_solver *s, const char *path, double t, double dt);
 int ebb_load_solution(ebb_solver *s, const char *path);
 /* loadSolution of a partitioned run (io.d:218-366): every file's cells go to their

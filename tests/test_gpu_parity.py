@@ -1,6 +1,6 @@
 """CUDA path vs the oracle, through the C ABI (GPU).
 
-Bar (the benchmark spec): plain FP64 GPU residual within 1e-12 relative per cell after one
+Bar: plain FP64 GPU residual within 1e-12 relative per cell after one
 stage, state within 1e-9 relative after 100 steps.  The FP64 kernels keep the
 reference's operation order without fused multiply-adds, so most cases agree
 bitwise; the constant-pressure ghost state uses CUDA's pow(), which may differ from
