@@ -607,6 +607,7 @@ def run_serve(args):
     nxt = 0
     ids = {}
     done = {}
+    states = {}
     while len(done) < R:
         now = time.perf_counter() - tb
         while nxt < R and arrivals[nxt] <= now:
@@ -618,7 +619,7 @@ def run_serve(args):
             r["latency_s"] = time.perf_counter() - tb - arrivals[k]
             done[k] = r
             if r["status"] == 0:
-                sv.take_state(r["id"])
+                states[k] = sv.take_state(r["id"])
         if a == 0:
             time.sleep(0.001)
     wall = time.perf_counter() - tb
@@ -631,6 +632,27 @@ def run_serve(args):
     # sequential plain FP64: per-step device time alone x steps run
     per = seq_ms_per_step(L, E, meshes, cfgs, "fp64", args.seq_steps, 3)
     seq_s = float(sum(per[k] * iters[k] for k in range(R)) / 1e3)
+    # error of the served (split) results against plain FP64 solves with the same stop
+    # conditions, on the smallest requests (three bump channels, one cylinder: their
+    # FP64 re-solves take seconds)
+    err = []
+    picks = [k for k in sorted(states, key=lambda k: meshes[k].n_cells) if kinds[k] == "bump"][:3] + \
+        [k for k in sorted(states, key=lambda k: meshes[k].n_cells) if kinds[k] == "cyl"][:1]
+    for k in picks:
+        s64 = E.UfvmSolver(meshes[k], cfgs[k], "fp64")
+        s64.set_stop(0, t_end=cfgs[k].t_end, max_steps=cap, resid_drop=1e-8)
+        row = {"k": int(k), "kind": str(kinds[k]), "cells": meshes[k].n_cells, "iterations": int(iters[k])}
+        try:
+            s64.run(10 ** 7, records=False)
+            q64, q32 = s64.state, states[k]
+            row["fp64_iterations"] = int(s64.status()[0]["iterations"])
+            row["l2_rel"] = [float(x) for x in np.sqrt(((q32 - q64) ** 2).mean(axis=0)
+                                                       / np.maximum((q64 ** 2).mean(axis=0), 1e-300))]
+            row["max_rel"] = float((np.abs(q32 - q64).max(axis=0) / np.maximum(np.abs(q64).max(axis=0), 1e-300)).max())
+        except E.EbbError as ex:
+            row["fp64_error"] = str(ex)[:120]
+        s64.close()
+        err.append(row)
     return {"workload": "served-bump70-cyl30-split", "integrator": args.serve_integrator,
             "bump_flux": args.serve_flux, "requests": R,
             "arrival_rate_per_s": 40.0,
@@ -647,7 +669,7 @@ def run_serve(args):
                                 "sample": "%d timed steps per request alone after 3 warm-up, x steps run"
                                           % args.seq_steps},
             "throughput_vs_sequential_fp64": (cu / wall) / (cu / seq_s), "bytes_peak": stats["bytes_peak"],
-            "mesh_s": round(mesh_s, 1), "clocks": clk}
+            "error_vs_fp64": err, "mesh_s": round(mesh_s, 1), "clocks": clk}
 
 
 def run_reference(args, ws, rank):
