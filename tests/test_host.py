@@ -375,3 +375,29 @@ def test_integer_pipe_conversions_match_ieee(tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
     n, bad = int(out[-2]), int(out[-1])
     assert n > 8_000_000 and bad == 0, " ".join(out[:-2])
+
+
+def test_hanging_node_polygons():
+    """The non-conforming quad mesh used by the six-neighbour parity case: 14 pentagons
+    and one hexagon among the quads, counter-clockwise and tiling the unit square; the
+    product's mesh import and the oracle's restatement agree on cells and edges."""
+    from oracle import ref
+    from tests.cases import cfg_json
+    g = meshgen.hanging_quads(16)
+    els = g.element_list()
+    sizes = np.bincount([len(e) for e in els])
+    assert sizes[4] == 817 and sizes[5] == 14 and sizes[6] == 1
+    area = 0.0
+    for e in els:
+        p = g.nodes[np.asarray(e) - 1]
+        a = 0.5 * np.sum(p[:, 0] * np.roll(p[:, 1], -1) - np.roll(p[:, 0], -1) * p[:, 1])
+        assert a > 0
+        area += a
+    assert abs(area - 1.0) < 1e-12
+    m = g.to_solver_mesh()
+    assert m.info.max_edges == 6 and m.n_cells == len(els)
+    text = cfg_json(initialConditions=[0.5, 0, 1, 1],
+                    boudaryConditions=[{"tag": "Freestream", "type": "dirichlet", "q": [0.5, 0, 1, 1]}])
+    om = ref.OracleMesh(g.as_reader_dict(), gmsh_ref.load_config(text), mms=2)
+    assert om.n_cells == m.n_cells and om.n_bnd == len(g.b_nodes)
+    assert om.n_int == m.info.n_int_edges
