@@ -401,3 +401,27 @@ def test_hanging_node_polygons():
     om = ref.OracleMesh(g.as_reader_dict(), gmsh_ref.load_config(text), mms=2)
     assert om.n_cells == m.n_cells and om.n_bnd == len(g.b_nodes)
     assert om.n_int == m.info.n_int_edges
+
+
+def test_bench_roofline_inputs():
+    """bench.py's roofline inputs: the committed ncu summaries carry DRAM traffic for
+    every stage kernel of both precision forms (scaled by cell count), and the
+    algorithmic-bytes model counts the split update's freestream-correction reads."""
+    import sys
+    sys.path.insert(0, ROOT)
+    import bench
+    for kern in ("k_cell", "k_flux", "k_update"):
+        for prec in ("fp64", "split"):
+            t = bench.profiled_traffic(kern, prec, bench.PROFILED_CELLS)
+            assert t is not None and t["bytes"] > 1e7, (kern, prec)
+            n = bench.PROFILED_CELLS // 2
+            half = bench.profiled_traffic(kern, prec, n)
+            assert abs(half["bytes"] - t["bytes"] * n / bench.PROFILED_CELLS) <= 1.0
+
+    class Info:
+        n_cells, face_slots, n_int_edges, n_ghost = 1000, 3000, 1480, 40
+    b64 = bench.algorithmic_bytes(Info, real=8)
+    b32 = bench.algorithmic_bytes(Info, real=4)
+    assert all(v > 0 for v in b64.values()) and b32["cell"] < b64["cell"]
+    plain32 = Info.n_cells * (4 + 12 + 32 + 16 + 16) + Info.face_slots * 4 + (Info.n_int_edges + Info.n_ghost) * 20
+    assert b32["update"] == plain32 + Info.n_cells * 16 + Info.face_slots * 12
