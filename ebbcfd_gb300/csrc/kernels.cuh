@@ -18,9 +18,11 @@
 //             +-1 multipliers in the cell's own edge order (the reference's summation
 //             order), CFL time step, Rmax, -1/area scaling (solve.d:1080-1121), the
 //             manufactured source, and the integrator stage combination
-//             (integrators.d), with min/max/sum reductions in fixed-order trees.
+//             (integrators.d), with min/max/sum reductions in fixed-order trees;
+//             split path: the freestream correction (uniform flow stays uniform).
 // Accumulation is atomic-free (gather, not scatter); the only atomics are the
-// order-independent min/max of dt and Rmax and the first-error key.
+// order-independent min/max of dt and Rmax and the first-error key.  All three and
+// the step epilogue use programmatic dependent launch (grid_dep_wait below).
 #pragma once
 
 #include <cuda_runtime.h>
