@@ -425,3 +425,33 @@ def test_bench_roofline_inputs():
     assert all(v > 0 for v in b64.values()) and b32["cell"] < b64["cell"]
     plain32 = Info.n_cells * (4 + 12 + 32 + 16 + 16) + Info.face_slots * 4 + (Info.n_int_edges + Info.n_ghost) * 20
     assert b32["update"] == plain32 + Info.n_cells * 16 + Info.face_slots * 12
+
+
+def test_wedge_mesh_quality_and_count():
+    """The benchmark wedge generator: Poisson-disk points give no poorly shaped
+    triangle (quality 4 sqrt(3) area / sum of squared edges above 0.35), the triangle
+    count lands within 2% of the request, and every boundary edge lies on the domain
+    outline with the tag of its segment."""
+    n = 20000
+    g = meshgen.wedge(n, seed=0)
+    tr = np.asarray(g.elements) - 1
+    p = g.nodes[tr]
+    a = 0.5 * ((p[:, 1, 0] - p[:, 0, 0]) * (p[:, 2, 1] - p[:, 0, 1]) - (p[:, 2, 0] - p[:, 0, 0]) * (p[:, 1, 1] - p[:, 0, 1]))
+    l2 = ((p[:, 1] - p[:, 0]) ** 2).sum(1) + ((p[:, 2] - p[:, 1]) ** 2).sum(1) + ((p[:, 0] - p[:, 2]) ** 2).sum(1)
+    assert (a > 0).all() and (4 * np.sqrt(3) * a / l2).min() > 0.35
+    assert abs(len(tr) / n - 1) < 0.02
+    ta = np.tan(np.radians(15.0))
+    starts = list(g.b_group_start) + [len(g.b_nodes)]
+    for t, tag in enumerate(g.tags):
+        mid = g.nodes[g.b_nodes[starts[t]:starts[t + 1]]].mean(axis=1)
+        x, y = mid[:, 0], mid[:, 1]
+        if tag == "Inflow":
+            assert np.allclose(x, 0)
+        elif tag == "Outflow":
+            assert np.allclose(x, 3)
+        elif tag == "Top":
+            assert np.allclose(y, 1)
+        elif tag == "Symmetry":
+            assert np.allclose(y, 0) and (x <= 0.5 + 1e-12).all()
+        elif tag == "Ramp":
+            assert np.allclose(y, (x - 0.5) * ta) and (x >= 0.5 - 1e-12).all()
