@@ -12,8 +12,8 @@ so no flush is needed between steps.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 --impl reference times the reference-semantics FP64 CPU restatement (oracle/) on all
-host cores on the same mesh and config (the D reference cannot be built on this
-machine or the GPU host: no D compiler, MPI or ParMETIS).  N>1: one independent
+host cores on the same mesh and config (the D reference cannot be built: no D
+compiler, MPI or ParMETIS is installed).  N>1: one independent
 replica per GPU (the path does not shard), weak scaling.
 """
 import argparse
