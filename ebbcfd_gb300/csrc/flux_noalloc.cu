@@ -1,11 +1,18 @@
 // flux_noalloc.cu -- batched face-flux evaluation that allocates no device memory.
 //
-// ebb_flux stages its host arrays through device buffers it allocates on every call.
-// This variant stages them through one fixed array compiled into the library
-// (EBB_FLUX_NOALLOC_MAX faces, 15 doubles per face: 3.75 MiB on every GPU that loads
-// the library, held until the process exits), so a caller that cannot allocate
-// device memory at call time can still evaluate fluxes.  Compiled with -fmad=false
+// ebb_flux stages its host arrays through device buffers it allocates and frees on
+// every call.  Some callers cannot do that: a process that shares the GPU with
+// running solves (cudaFree synchronises the whole device, stalling every stream the
+// solves run on), or one whose device memory is already reserved, e.g. by a request
+// server's HBM budget.  This variant stages through one fixed array compiled into the
+// library (EBB_FLUX_NOALLOC_MAX faces, 15 doubles per face: 3.75 MiB on every GPU
+// that loads the library, held until the process exits).  Compiled with -fmad=false
 // like the plain FP64 kernels: results are bitwise those of ebb_flux.
+//
+// Set-up, once per device on the first call with that device current: the array's
+// device address (cudaGetSymbolAddress: in host code the array's name is only a
+// stand-in) and a non-blocking stream the copies and the kernel run on.  Every later
+// call on the device only copies, launches and waits on that stream.
 //
 // The array is shared by every call on a device and keeps the last call's contents;
 // each call overwrites the whole region it reads, so nothing needs clearing.  Calls
@@ -25,7 +32,11 @@ constexpr int kMaxDevices = 64;
 __device__ __align__(256) double g_flux_scratch[15 * EBB_FLUX_NOALLOC_MAX];
 
 std::mutex g_mu;
-double *g_scratch_ptr[kMaxDevices] = {};
+struct DeviceScratch {
+    double *base = nullptr;
+    cudaStream_t stream = nullptr;
+};
+DeviceScratch g_dev[kMaxDevices];
 
 __global__ void k_flux_scratch(int kind, int64_t n, double *base)
 {
@@ -41,21 +52,24 @@ __global__ void k_flux_scratch(int kind, int64_t n, double *base)
     s[i] = sm;
 }
 
-// Device address of the scratch array on the current device: the host-side symbol
-// is only a stand-in, so the address is looked up once per device with that device
-// current and cached.
-int scratch_for_current_device(double **out)
+// The scratch array's device address and the stream of the current device, set up
+// on the device's first call (with that device current) and cached.
+int scratch_for_current_device(DeviceScratch *out)
 {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return EBB_ERR_NO_DEVICE;
     if (dev >= kMaxDevices) return EBB_ERR_LIMIT;
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_ptr[dev]) {
+    DeviceScratch &d = g_dev[dev];
+    if (!d.base) {
         double *p = nullptr;
         if (cudaGetSymbolAddress((void **)&p, g_flux_scratch) != cudaSuccess || !p) return EBB_ERR_CUDA;
-        g_scratch_ptr[dev] = p;
+        cudaStream_t st = nullptr;
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return EBB_ERR_CUDA;
+        d.stream = st;
+        d.base = p;
     }
-    *out = g_scratch_ptr[dev];
+    *out = d;
     return EBB_OK;
 }
 
@@ -69,17 +83,24 @@ extern "C" int ebb_flux_noalloc(int32_t kind, int64_t n, const double *qL, const
     if (n == 0) return EBB_OK;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return EBB_ERR_NO_DEVICE;
-    double *base = nullptr;
-    int r = scratch_for_current_device(&base);
+    DeviceScratch d;
+    int r = scratch_for_current_device(&d);
     if (r) return r;
-    cudaError_t e = cudaMemcpy(base, qL, sizeof(double) * 4 * n, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(base + 4 * kMax, qR, sizeof(double) * 4 * n, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(base + 8 * kMax, normal, sizeof(double) * 2 * n, cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) return EBB_ERR_CUDA;
-    const int T = 128;
-    k_flux_scratch<<<(unsigned)((n + T - 1) / T), T>>>(kind, n, base);
-    e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaMemcpy(F, base + 10 * kMax, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess) e = cudaMemcpy(s_max, base + 14 * kMax, sizeof(double) * n, cudaMemcpyDeviceToHost);
-    return e == cudaSuccess ? EBB_OK : EBB_ERR_CUDA;
+    double *base = d.base;
+    cudaStream_t st = d.stream;
+    cudaError_t e = cudaMemcpyAsync(base, qL, sizeof(double) * 4 * n, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(base + 4 * kMax, qR, sizeof(double) * 4 * n, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(base + 8 * kMax, normal, sizeof(double) * 2 * n, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        const int T = 128;
+        k_flux_scratch<<<(unsigned)((n + T - 1) / T), T, 0, st>>>(kind, n, base);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(F, base + 10 * kMax, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s_max, base + 14 * kMax, sizeof(double) * n, cudaMemcpyDeviceToHost, st);
+    // wait for whatever was enqueued, also after a failed enqueue, so that no copy into
+    // the caller's buffers is still pending when the call returns
+    const cudaError_t w = cudaStreamSynchronize(st);
+    return (e == cudaSuccess && w == cudaSuccess) ? EBB_OK : EBB_ERR_CUDA;
 }

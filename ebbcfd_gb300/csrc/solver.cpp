@@ -30,6 +30,21 @@ int fail(ebb_solver *s, int code, const std::string &msg)
         cudaError_t _e = (x);                                                                  \
         if (_e != cudaSuccess) return fail(s, cuda_status(_e), std::string("CUDA: ") + cudaGetErrorString(_e)); \
     } while (0)
+// Two CUDA events, destroyed on every return path of the function that holds them.
+struct EventPair {
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaError_t create()
+    {
+        cudaError_t e = cudaEventCreate(&ev[0]);
+        return e == cudaSuccess ? cudaEventCreate(&ev[1]) : e;
+    }
+    ~EventPair()
+    {
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+};
+
 #define CKL(x)                                                                                 \
     do {                                                                                       \
         int _r = (x);                                                                          \
@@ -262,9 +277,9 @@ template <typename T> int profile_t(ebb_solver *s, int32_t n_rep, double *ms)
     CK(cudaMemcpyAsync(s->A.qs, s->A.qs1, bytes, cudaMemcpyDeviceToDevice, s->stream));
     T *qs = reinterpret_cast<T *>(s->A.qs);
     T *scratch = reinterpret_cast<T *>(s->A.face);  // update output target (rebuilt below)
-    cudaEvent_t ev[2];
-    CK(cudaEventCreate(&ev[0]));
-    CK(cudaEventCreate(&ev[1]));
+    EventPair evp;
+    CK(evp.create());
+    cudaEvent_t *ev = evp.ev;
     for (int k = 0; k < 4; k++) {
         float t = 0;
         CK(cudaEventRecord(ev[0], s->stream));
@@ -280,8 +295,6 @@ template <typename T> int profile_t(ebb_solver *s, int32_t n_rep, double *ms)
         ms[k] = (double)t / n_rep;
         if (k == 2) CKL(launch_cell<T>(s->M, s->P, s->A, qs, 1, s->stream));
     }
-    cudaEventDestroy(ev[0]);
-    cudaEventDestroy(ev[1]);
     return EBB_OK;
 }
 
@@ -567,17 +580,15 @@ int ebb_run_timed(ebb_solver *s, int64_t max_steps, int64_t *steps_run, double *
     if ((r = ensure_graphs(s))) return r;
     std::vector<int64_t> it0(s->n_inst);
     for (int k = 0; k < s->n_inst; k++) it0[k] = h[k].iter;
-    cudaEvent_t ev[2];
-    CK(cudaEventCreate(&ev[0]));
-    CK(cudaEventCreate(&ev[1]));
+    EventPair evp;
+    CK(evp.create());
+    cudaEvent_t *ev = evp.ev;
     CK(cudaEventRecord(ev[0], s->stream));
     if ((r = enqueue_steps(s, max_steps))) return r;
     CK(cudaEventRecord(ev[1], s->stream));
     CK(cudaEventSynchronize(ev[1]));
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, ev[0], ev[1]));
-    cudaEventDestroy(ev[0]);
-    cudaEventDestroy(ev[1]);
     *device_ms = ms;
     if ((r = solver_sync_all(s, h))) return r;
     int64_t did = 0;
@@ -630,6 +641,25 @@ int ebb_get_face_states(ebb_solver *s, double *out)
     return EBB_OK;
 }
 
+int ebb_get_edge_fluxes(ebb_solver *s, double *out)
+{
+    if (!s || !out || s->n_inst != 1) return EBB_ERR_ARG;
+    const size_t n = 4 * (size_t)(s->Eint + s->G);
+    std::vector<double> f(n);
+    if (s->precision == EBB_PREC_SPLIT) {
+        std::vector<float> g(n);
+        CK(cudaMemcpyAsync(g.data(), s->A.fl, n * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        for (size_t k = 0; k < n; k++) f[k] = g[k];
+    } else {
+        CK(cudaMemcpyAsync(f.data(), s->A.fl, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
+    for (size_t e = 0; e < s->flux_ref.size(); e++)
+        for (int c = 0; c < 4; c++) out[4 * (size_t)s->flux_ref[e] + c] = f[4 * e + c];
+    return EBB_OK;
+}
+
 int ebb_flux(int32_t kind, int64_t n, const double *qL, const double *qR, const double *normal, double *F, double *s_max)
 {
     if (n < 0 || (n && (!qL || !qR || !normal || !F || !s_max))) return EBB_ERR_ARG;
@@ -641,12 +671,13 @@ int ebb_flux(int32_t kind, int64_t n, const double *qL, const double *qR, const 
     size_t tot = (size_t)n * (4 + 4 + 2 + 4 + 1);
     CK(cudaMalloc(&d, tot * sizeof(double)));
     double *dL = d, *dR = d + 4 * n, *dn = d + 8 * n, *dF = d + 10 * n, *ds = d + 14 * n;
-    cudaMemcpy(dL, qL, sizeof(double) * 4 * n, cudaMemcpyHostToDevice);
-    cudaMemcpy(dR, qR, sizeof(double) * 4 * n, cudaMemcpyHostToDevice);
-    cudaMemcpy(dn, normal, sizeof(double) * 2 * n, cudaMemcpyHostToDevice);
-    int r = launch_flux_batch(kind, n, dL, dR, dn, dF, ds, nullptr);
-    cudaError_t e = cudaMemcpy(F, dF, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess) e = cudaMemcpy(s_max, ds, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    // the kernel runs only on inputs that arrived: the first failed upload ends the call
+    cudaError_t e = cudaMemcpy(dL, qL, sizeof(double) * 4 * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dR, qR, sizeof(double) * 4 * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dn, normal, sizeof(double) * 2 * n, cudaMemcpyHostToDevice);
+    int r = e == cudaSuccess ? launch_flux_batch(kind, n, dL, dR, dn, dF, ds, nullptr) : 0;
+    if (e == cudaSuccess && !r) e = cudaMemcpy(F, dF, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && !r) e = cudaMemcpy(s_max, ds, sizeof(double) * n, cudaMemcpyDeviceToHost);
     cudaFree(d);
     if (r || e != cudaSuccess) return EBB_ERR_CUDA;
     return EBB_OK;

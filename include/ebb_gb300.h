@@ -175,6 +175,12 @@ int ebb_mesh_get_info(const ebb_mesh *mesh, ebb_mesh_info *info);
 int ebb_mesh_get_tag(const ebb_mesh *mesh, int32_t i, char *tag, size_t len);
 /* element centroids in reference cell order (cx, cy), for initial conditions and error norms */
 int ebb_mesh_centroids(const ebb_mesh *mesh, double *xy);
+/* The reference's edges (mesh.d:242-313: creation order, interior and boundary mixed),
+   n_edges of them: group[e] = boundary tag index or -1 for an interior edge;
+   cells[2e], cells[2e+1] = cellIdx[0] (the creating element) and cellIdx[1] (the other
+   element, or n_cells + ghost index on a boundary); mid, normal (2 per edge, pointing
+   out of cellIdx[0]) and len.  Any output may be NULL. */
+int ebb_mesh_edges(const ebb_mesh *mesh, int32_t *group, int32_t *cells, double *mid, double *normal, double *len);
 void ebb_mesh_free(ebb_mesh *mesh);
 
 /* ---- solver (buildMesh + ufvmSetup) ------------------------------------ */
@@ -215,6 +221,13 @@ int ebb_run_timed(ebb_solver *s, int64_t max_steps, int64_t *steps_run, double *
 /* Face states of the last residual evaluation per cell and local edge, reference order
    (the edge values .esln v2 stores, io.d:111-133): out[face_slots][4]. */
 int ebb_get_face_states(ebb_solver *s, double *out);
+
+/* len * flux of every edge from the last residual evaluation, at its reference edge id
+   (ebb_mesh_edges order): out[n_edges][4].  These are the terms the residual sums and
+   computeBoundaryForces adds up over the force tags (mesh.d:645-671: edge.flux * len),
+   e.g. the wall shear of a viscous wall is out[e][1] / len.  Single solves only
+   (EBB_ERR_ARG for a batched arena). */
+int ebb_get_edge_fluxes(ebb_solver *s, double *out);
 
 /* The CUDA stream (cudaStream_t) the solver launches on, for callers that time or
    order work around it with CUDA events. */
@@ -344,16 +357,18 @@ void ebb_server_destroy(ebb_server *sv);
 int ebb_flux(int32_t kind, int64_t n, const double *qL, const double *qR, const double *normal, double *F,
              double *s_max);
 /* Same evaluation and results as ebb_flux, for callers that cannot allocate device
-   memory when they call: ebb_flux allocates (and frees) device staging buffers on
-   every call, which is not allowed for example while another thread is capturing a
-   CUDA graph on the device in the global capture mode, and fails when a serving
-   process has reserved all device memory for its solver arenas.  This variant has no
-   counterpart in the reference.  It stages through one fixed array compiled into the
-   library (EBB_FLUX_NOALLOC_MAX faces, 3.75 MiB held on every GPU that loads the
-   library until the process exits) and returns EBB_ERR_LIMIT for n larger than
-   EBB_FLUX_NOALLOC_MAX.  Its first call on a device looks up the array's device
-   address for that device; make that first call before any stream capture.  Calls
-   share the array: calls that overlap on the same GPU race and must be serialised. */
+   memory when they call.  This variant has no counterpart in the reference.  ebb_flux
+   allocates and frees device staging buffers on every call; a caller that shares the
+   GPU with running solves cannot afford that (cudaFree synchronises the whole device
+   and stalls every stream the solves run on), and in a process whose device memory is
+   already reserved (a request server's HBM budget) the allocation fails.  This
+   variant stages through one fixed array compiled into the library
+   (EBB_FLUX_NOALLOC_MAX faces, 3.75 MiB held on every GPU that loads the library until
+   the process exits) and returns EBB_ERR_LIMIT, touching no output, for n larger than
+   EBB_FLUX_NOALLOC_MAX.  Its first call on a device sets up that device (the array's
+   device address and a non-blocking stream the call runs on); make that first call
+   before any stream capture.  Calls share the array, which keeps the last call's
+   contents: calls that overlap on the same GPU race and must be serialised. */
 int ebb_flux_noalloc(int32_t kind, int64_t n, const double *qL, const double *qR, const double *normal, double *F,
                      double *s_max);
 

@@ -1,9 +1,9 @@
 #!/usr/bin/env python3
 """Regenerate the committed golden fixtures under tests/golden/ from the EbbCFD tree.
 
-Run in a container that has the reference mounted (default /root/reference):
+Run where the EbbCFD tree is available, giving its location:
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref <EbbCFD tree>
 
 Outputs (all committed; nothing at test time reads the reference tree):
   roe_kat.json        the four Roe-flux known answers of source/flux.d:143-219,
@@ -74,7 +74,7 @@ def parse_plot_conv(path):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", required=True, help="root of the EbbCFD source tree")
     a = ap.parse_args()
     kat = parse_roe_kat(os.path.join(a.ref, "source", "flux.d"))
     assert len(kat) == 4 and all(len(c["F"]) == 4 for c in kat), kat

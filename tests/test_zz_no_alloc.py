@@ -1,9 +1,10 @@
 """The allocation-free flux entry point (ebb_flux_noalloc) against ebb_flux (GPU).
 
-Callers that cannot allocate device memory when they call (a thread running while
-another captures a CUDA graph in the global capture mode, a serving process whose
-device memory is all reserved) use ebb_flux_noalloc, which stages through a fixed
-array compiled into the library instead of allocating.  This file is collected last
+Callers that cannot allocate device memory when they call (a process sharing the GPU
+with running solves, where cudaFree would synchronise the device and stall them; a
+serving process whose device memory is all reserved) use ebb_flux_noalloc, which
+stages through a fixed array compiled into the library instead of allocating.  This
+file is collected last
 so that a run stopping at the first failure has already run every other test; it
 also passes on its own in a fresh process.
 """
@@ -59,3 +60,23 @@ def test_noalloc_rejects_sizes_beyond_its_limit():
     code, F, s = _call(L.ebb_flux_noalloc, 1, qL, qL, nrm)
     assert code == 12  # EBB_ERR_LIMIT
     assert np.isnan(F).all() and np.isnan(s).all()
+
+
+def test_noalloc_call_leaves_free_device_memory_unchanged():
+    """After the first call on the device (its set-up), a call of the largest size
+    takes no device memory: the free memory the driver reports is the same before and
+    after it."""
+    torch = pytest.importorskip("torch")
+    L = _lib.load()
+    rng = np.random.default_rng(7)
+    n = _lib.FLUX_NOALLOC_MAX
+    qL, qR, nrm = _states(rng, n)
+    code, F0, s0 = _call(L.ebb_flux_noalloc, 1, qL, qR, nrm)  # set-up call
+    assert code == 0
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    code, F1, s1 = _call(L.ebb_flux_noalloc, 1, qL, qR, nrm)
+    torch.cuda.synchronize()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert code == 0 and free1 == free0
+    assert np.array_equal(F1, F0) and np.array_equal(s1, s0)
