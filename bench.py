@@ -1,28 +1,35 @@
 #!/usr/bin/env python3
 """Throughput of the explicit unstructured FV update on GB300.
 
-Workload (default): the Mach 2.5 supersonic wedge -- [0,3]x[0,1] with a 15-degree
-ramp from x=0.5, ~1.0M seeded-Delaunay triangles graded 2x toward the ramp (seed 0),
-Rusanov flux, limited second order, RK2 at CFL 0.4, plain FP64.  A step is one RK2
-time step of the whole mesh (two residual evaluations + stage updates + the
-per-step reductions of the time loop); the metric is cell-updates/s = cells x
-steps / time.  The ~1M-cell state and face arrays (~0.5 GB) exceed the 129 MB L2,
-so no flush is needed between steps.
+Workload (default): the laminar Navier-Stokes flat plate -- domain [-0.5,2]x[0,0.5],
+4.0M mixed cells (anisotropic wall-layer quads, first-cell height 1e-4, growth 1.05;
+seeded-Delaunay triangles above), Mach 0.3, Re_L 1e5, Pr 0.72, adiabatic no-slip wall
+for x >= 0, Roe + viscous flux, limited second order, RK4 at CFL 0.8.  A step is one
+RK4 time step of the whole mesh (four residual evaluations with their stage updates,
+then the per-step reductions of the time loop); the metric is cell-updates/s = cells
+x steps / time.  `value` is the plain FP64 path (the reference's own precision and
+operation order); `split_path` beside it is the FP32/FP64 split precision form from
+the same initial state, with its speed-up and its error against FP64 for drag, lift,
+the wall skin friction, the residual history and the state.  The ~4M-cell working set
+(~2.4 GB FP64) exceeds the 129 MB L2, so no flush is needed between steps.  `wedge`
+repeats the measurement on the 1.0M-cell Mach 2.5 wedge (Rusanov, RK2, CFL 0.4).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 --impl reference times the reference-semantics FP64 CPU restatement (oracle/) on all
-host cores on the same mesh and config (the D reference cannot be built: no D
-compiler, MPI or ParMETIS is installed).  N>1: one independent
-replica per GPU (the path does not shard), weak scaling.
+host cores on the same plate mesh and config (the D reference cannot be built: no D
+compiler, MPI or ParMETIS is installed).  N>1: one independent replica per GPU (the
+path does not shard), weak scaling.
 """
 import argparse
+import ctypes
 import json
 import os
 import statistics
 import subprocess
 import sys
 import tempfile
+import threading
 import time
 
 import numpy as np
@@ -36,11 +43,41 @@ WEDGE_BCS = [{"tag": "Inflow", "type": "fullState", "q": [2.5, 0, 1, 1]},
              {"tag": "Ramp", "type": "inviscidWall", "q": [2.5, 0, 1, 1]},
              {"tag": "Outflow", "type": "fullState", "q": [2.5, 0, 1, 1]}]
 
+PLATE_WORKLOAD = "ns-plate-M0.3-Re1e5-roe-visc-rk4-cfl0.8"
+WEDGE_WORKLOAD = "wedge-M2.5-rusanov-rk2-cfl0.4"
+
 
 def wedge_config(cfl=0.4):
     return json.dumps({"mesh": "wedge.msh", "dt": 1e-4, "tEnd": 1e9, "flux": "rusanovFlux", "saveIter": -1,
                        "plotIter": -1, "forceBoundary": "Ramp", "integrator": "RK2", "limited": True, "CFL": cfl,
                        "initialConditions": [2.5, 0, 1, 1], "boudaryConditions": WEDGE_BCS})
+
+
+def plate_config():
+    bcs = [{"tag": "Inflow", "type": "fullState", "q": [0.3, 0, 1, 1]},
+           {"tag": "Top", "type": "fullState", "q": [0.3, 0, 1, 1]},
+           {"tag": "Outflow", "type": "constP", "q": [1.0 / (1.4 * 0.09)]},
+           {"tag": "Symmetry", "type": "symmetry", "q": [0.3, 0, 1, 1]},
+           {"tag": "Wall", "type": "viscidWall", "q": [0.3, 0, 1, 1]}]
+    return json.dumps({"mesh": "plate.msh", "dt": 1e-7, "tEnd": 1e9, "flux": "roeFlux", "saveIter": -1,
+                       "plotIter": -1, "forceBoundary": "Wall", "integrator": "RK4", "limited": True, "CFL": 0.8,
+                       "cflAdjust": False, "viscosity": True,
+                       "physicalConfig": {"Pr": 0.72, "R": 1.0, "gamma": 1.4, "Re": 1e5, "L": 1.0},
+                       "initialConditions": [0.3, 0, 1, 1], "boudaryConditions": bcs})
+
+
+# what each headline workload runs: mesh generator, config, force tag, stages per step
+WORKLOADS = {
+    "plate": {"name": PLATE_WORKLOAD, "cells": 4_000_000, "config": plate_config, "force_tag": "Wall",
+              "stages": 4, "need_grad": True, "integrator": "RK4"},
+    "wedge": {"name": WEDGE_WORKLOAD, "cells": 1_000_000, "config": wedge_config, "force_tag": "Ramp",
+              "stages": 2, "need_grad": False, "integrator": "RK2"},
+}
+
+
+def make_mesh(kind, cells):
+    from ebbcfd_gb300 import meshgen
+    return meshgen.flat_plate(cells) if kind == "plate" else meshgen.wedge(cells, seed=0)
 
 
 def max_over_ranks(x):
@@ -62,48 +99,98 @@ def dist_env():
 
 
 class Clocks:
-    """nvidia-smi samples during the timed region."""
+    """SM clock, its maximum, power and the active clock-event reasons of the GPU,
+    sampled every 2 ms by a host thread during the timed region through NVML's
+    read-only queries (libnvidia-ml, loaded with ctypes); nvidia-smi at 50 ms when NVML
+    cannot be loaded.  The timed calls release the interpreter lock (ctypes), so the
+    thread samples while the GPU works."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
+    REASONS = {0x2: "applications_clocks_setting", 0x4: "sw_power_cap", 0x8: "hw_slowdown",
+               0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
 
     def __init__(self, device):
         self.device = device
+        self.rows = []
+        self.src = None
+        self._stop = threading.Event()
+        self._t = None
         self.p = None
-        self.f = None
+
+    def _nvml_handle(self):
+        nv = ctypes.CDLL("libnvidia-ml.so.1")
+        if nv.nvmlInit_v2() != 0:
+            return None, None
+        h = ctypes.c_void_p()
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")
+        sel = vis[self.device].strip() if vis and vis[0] != "" and self.device < len(vis) else str(self.device)
+        if sel.startswith("GPU-") or sel.startswith("MIG-"):
+            r = nv.nvmlDeviceGetHandleByUUID(sel.encode(), ctypes.byref(h))
+        else:
+            r = nv.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(int(sel)), ctypes.byref(h))
+        return (nv, h) if r == 0 else (None, None)
+
+    def _run_nvml(self, nv, h):
+        sm, mx, pw, rs = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+        reasons = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        while not self._stop.is_set():
+            if nv.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(sm)) == 0 and \
+                    nv.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0:
+                ok_r = reasons(h, ctypes.byref(rs)) == 0
+                ok_p = nv.nvmlDeviceGetPowerUsage(h, ctypes.byref(pw)) == 0
+                self.rows.append((float(sm.value), float(mx.value), pw.value / 1e3 if ok_p else None,
+                                  int(rs.value) if ok_r else 0))
+            time.sleep(0.002)
 
     def start(self):
         try:
+            nv, h = self._nvml_handle()
+        except OSError:
+            nv, h = None, None
+        if nv is not None:
+            self.src = "nvml, 2 ms"
+            self._t = threading.Thread(target=self._run_nvml, args=(nv, h), daemon=True)
+            self._t.start()
+            return
+        try:
             self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
-                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                       "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.f,
                                       stderr=subprocess.DEVNULL)
+            self.src = "nvidia-smi, 50 ms"
         except Exception:
             self.p = None
 
     def stop(self):
-        if self.p is None:
+        if self._t is not None:
+            self._stop.set()
+            self._t.join()
+        elif self.p is not None:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+            self.f.flush()
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            bits = [0x8, 0x40, 0x20, 0x4]
+            for line in open(self.f.name):
+                r = [x.strip() for x in line.split(",")]
+                if len(r) >= 9 and r[1].replace(".", "").isdigit() and r[2].replace(".", "").isdigit():
+                    rs = sum(b for b, k in zip(bits, range(4)) if r[5 + k] == "Active")
+                    pw = float(r[3]) if r[3].replace(".", "").isdigit() else None
+                    self.rows.append((float(r[1]), float(r[2]), pw, rs))
+            os.unlink(self.f.name)
+        if not self.rows:
             return None
-        self.p.terminate()
-        try:
-            self.p.wait(timeout=5)
-        except Exception:
-            self.p.kill()
-        self.f.flush()
-        rows = []
-        for line in open(self.f.name):
-            parts = [x.strip() for x in line.split(",")]
-            if len(parts) >= 9:
-                rows.append(parts)
-        os.unlink(self.f.name)
-        if not rows:
-            return None
-        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k] == "Active"})
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+        sm = [r[0] for r in self.rows]
+        pw = [r[2] for r in self.rows if r[2] is not None]
+        reasons = sorted({n for r in self.rows for b, n in self.REASONS.items() if r[3] & b})
+        return {"sm_mhz": statistics.median(sm), "sm_min_mhz": min(sm), "sm_max_mhz": max(r[1] for r in self.rows),
+                "reasons": reasons, "samples": len(self.rows), "power_w_max": max(pw) if pw else None,
+                "source": self.src}
 
 
 def peaks():
@@ -114,34 +201,43 @@ def peaks():
     return 6800.0, "fallback"
 
 
-PROFILED_CELLS = 1_001_045  # the wedge the committed ncu captures ran on
-
-
-def profiled_traffic(kernel, precision, ncell):
-    """DRAM bytes (read + write) per launch of `kernel` from the committed ncu
-    summaries under profiles/ ("traffic: <kernel> <precision> <bytes>" lines, one
-    capture of the 1,001,045-cell wedge), scaled to `ncell` cells (traffic grows with
-    the cells processed); None when no capture covers the kernel."""
+def profiled_counters(kernel, precision, workload, ncell):
+    """DRAM bytes (read + write) per launch of `kernel` and its FP64-pipe share from the
+    committed ncu summaries under profiles/: lines "traffic: <kernel> <precision>
+    <bytes> <workload> <cells>" and "fp64pipe: <kernel> <precision> <percent>
+    <workload>" (a capture of `cells` cells of the workload; traffic is scaled to
+    `ncell` cells: it grows with the cells processed).  None when no capture covers the
+    kernel."""
     import glob
     import re
+    out = {"traffic": None, "fp64_pipe_pct": None}
     for f in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
         for line in open(f):
-            m = re.match(r"traffic: (\S+) (\S+) (\d+)\s*$", line)
-            if m and m.group(1) == kernel and m.group(2) == precision:
-                return {"bytes": int(m.group(3)) * ncell / PROFILED_CELLS, "source": os.path.relpath(f, ROOT),
-                        "scaled_from_cells": PROFILED_CELLS}
-    return None
+            m = re.match(r"traffic: (\S+) (\S+) (\d+) (\S+) (\d+)\s*$", line)
+            if m and m.group(1) == kernel and m.group(2) == precision and m.group(4) == workload:
+                cells = int(m.group(5))
+                out["traffic"] = {"bytes": int(m.group(3)) * ncell / cells, "source": os.path.relpath(f, ROOT),
+                                  "captured_cells": cells}
+            m = re.match(r"fp64pipe: (\S+) (\S+) ([\d.]+) (\S+)\s*$", line)
+            if m and m.group(1) == kernel and m.group(2) == precision and m.group(4) == workload:
+                out["fp64_pipe_pct"] = float(m.group(3))
+    return out
 
 
 def algorithmic_bytes(info, real=8, need_grad=False, limited=True):
     """Bytes each kernel must move per launch, every array touched once (re-reads of
     a neighbour's state count 0).  S = face slots, E = interior edges, G = boundary
-    edges; real = bytes of the arithmetic type (8 plain FP64, 4 split)."""
+    edges; real = bytes of the arithmetic type (8 plain FP64, 4 split).  need_grad:
+    viscous terms, k_cell writes each cell's gradient and k_flux reads it (with the
+    edge's two cell ids).  The update figure is a first RK stage (the stage
+    ebb_profile_kernels times)."""
     C, S, E, G = info.n_cells, info.face_slots, info.n_int_edges, info.n_ghost
     r = real
     cell = C * (4 * r + 4) + S * (4 + 2 * r + (2 * r if limited else 0) + 2 * r) + S * 4 * r + (C * 8 * r if need_grad else 0)
     flux = E * (8 + 2 * r + r + 8 * r + 5 * r) + G * (12 + 2 * r + r + 4 * r + 4 * r + 5 * r)
-    # residual + RK2 first-stage update: nedge, perim, d, -1/area, FP64 q read, aux write
+    if need_grad:
+        flux += E * 8 + (C + G) * 8 * r
+    # residual + first-stage update: nedge, perim, d, -1/area, FP64 q read, aux write
     # (T) and next-stage state write (T)
     update = C * (4 + 3 * r + 32 + 4 * r + 4 * r) + S * 4 + (E + G) * 5 * r
     if r == 4:  # split: the freestream correction reads the stage state and each slot's normal and length
@@ -149,15 +245,35 @@ def algorithmic_bytes(info, real=8, need_grad=False, limited=True):
     return {"cell": cell, "flux": flux, "update": update}
 
 
-def measure(L, E, _lib, gen, mesh, precision, args, local, ws, want_e2e):
+def wall_cf(edges, efl, tag_index):
+    """Skin friction of a viscous wall per wall edge: the wall shear is the x-momentum
+    flux F1 = len*F1 / len of each wall edge (the wall is y = 0, n = (0, -1), so
+    F1 = -Fv1 = mu du/dy), and Cf = shear / (0.5 rho U^2) with the freestream rho = U = 1.
+    Returns (x of the edge midpoints, Cf), sorted by x."""
+    m = edges["group"] == tag_index
+    x = edges["mid"][m, 0]
+    cf = 2.0 * efl[m, 1] / edges["len"][m]
+    o = np.argsort(x)
+    return x[o], cf[o]
+
+
+def rel_l2(a, b):
+    return float(np.sqrt(np.sum((a - b) ** 2) / max(np.sum(b ** 2), 1e-300)))
+
+
+def measure(L, E, _lib, mesh, wl, precision, args, local, ws, want_e2e, hist_steps):
+    """One precision form on one workload: `hist_steps` recorded steps (warm-up, and
+    the force and residual history), per-kernel event times, `args.steps` timed steps
+    (CUDA events on the solver stream, inputs resident), then the end-to-end run
+    through the C ABI with host copies every step."""
     import ctypes as C
-    cfg = E.load_config(wedge_config())
+    cfg = E.load_config(wl["config"]())
     t0 = time.time()
     sol = E.UfvmSolver(mesh, cfg, precision=precision)
     setup_s = time.time() - t0
     info = mesh.info
     ncell = info.n_cells
-    sol.run(args.warmup, records=False)
+    hist = sol.run(max(args.warmup, hist_steps), records=True)
     ms = (C.c_double * 4)()
     L.ebb_profile_kernels(sol.h, 20, ms)
     kern_ms = {"cell": ms[0], "flux": ms[1], "update": ms[2], "step_end": ms[3]}
@@ -176,6 +292,8 @@ def measure(L, E, _lib, gen, mesh, precision, args, local, ws, want_e2e):
     steps_done = n.value
     if ws > 1:
         elapsed = max_over_ranks(elapsed)
+    st = sol.status()[0]
+    efl = sol.edge_fluxes()
     state = sol.state
     value = ws * ncell * steps_done / elapsed
     e2e = None
@@ -200,76 +318,120 @@ def measure(L, E, _lib, gen, mesh, precision, args, local, ws, want_e2e):
         e2e = {"value": ws * ncell * k_e2e / t_e2e, "unit": "cell-updates/s", "h2d_bytes_per_step": nbytes,
                "d2h_bytes_per_step": nbytes + C.sizeof(_lib.StepRecord), "steps": k_e2e}
     peak, peak_kind = peaks()
-    ab = algorithmic_bytes(info, real=8 if precision == "fp64" else 4)
+    ab = algorithmic_bytes(info, real=8 if precision == "fp64" else 4, need_grad=wl["need_grad"])
+    kernels = {}
+    for k in ("cell", "flux", "update"):
+        sec = kern_ms[k] * 1e-3
+        cnt = profiled_counters("k_" + k, precision, wl["name"], ncell)
+        row = {"ms": kern_ms[k], "algorithmic_bytes": ab[k], "achieved_gbs": ab[k] / sec / 1e9,
+               "frac": ab[k] / sec / 1e9 / peak}
+        if cnt["traffic"]:
+            row["dram_bytes"] = cnt["traffic"]["bytes"]
+            row["dram_gbs"] = cnt["traffic"]["bytes"] / sec / 1e9
+            row["frac_dram"] = row["dram_gbs"] / peak
+            row["traffic_source"] = cnt["traffic"]
+        if cnt["fp64_pipe_pct"] is not None:
+            row["fp64_pipe_active_pct"] = cnt["fp64_pipe_pct"]
+        kernels["k_" + k] = row
     dom = max(("cell", "flux", "update"), key=lambda k: kern_ms[k])
-    achieved = ab[dom] / (kern_ms[dom] * 1e-3) / 1e9
-    tr = profiled_traffic("k_" + dom, precision, ncell)
-    roof = {"bound": "hbm", "kernel": "k_" + dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": peak_kind, "traffic": tr["bytes"] if tr else None,
-            "traffic_source": tr, "kernel_ms": kern_ms, "algorithmic_bytes": ab}
+    d = kernels["k_" + dom]
+    roof = {"bound": "hbm", "kernel": "k_" + dom, "achieved": d["achieved_gbs"], "peak": peak, "unit": "GB/s",
+            "frac": d["frac"], "achieved_basis": "algorithmic bytes per launch (model) / event-timed launch",
+            "frac_dram": d.get("frac_dram"), "peak_source": peak_kind, "traffic": d.get("dram_bytes"),
+            "kernels": kernels, "step_end_ms": kern_ms["step_end"]}
     if precision == "fp64":
-        # the FP64 kernels are bound by the FP64 pipe, not by HBM (ncu, profiles/fp64_wedge1m.md)
-        roof["fp64_pipe_active_pct"] = {"k_cell": 85.9, "k_flux": 86.8}
+        roof["limiter"] = "FP64 pipe (ncu fp64_pipe_active_pct; GB300 runs FP64 at a small fraction of FP32)"
     sol.close()
     return {"value": value, "elapsed": elapsed, "steps": steps_done, "setup_s": setup_s, "roofline": roof,
-            "e2e": e2e, "clocks": clk, "state": state}
+            "e2e": e2e, "clocks": clk, "state": state, "hist": hist, "status": st, "edge_fluxes": efl}
 
 
-def run_ours(args, ws, rank, local):
+def split_errors(mesh, wl, m64, m32):
+    """Error of the split precision form against plain FP64 from the same initial state
+    after the same steps: drag and lift, the force tag's wall shear (Cf per wall edge,
+    viscous walls), the recorded residual and force history, and the state."""
+    q64, q32 = m64["state"], m32["state"]
+    scale = np.maximum(np.abs(q64).max(axis=0), 1e-300)
+    h64, h32 = m64["hist"], m32["hist"]
+    nh = min(len(h64), len(h32))
+    r64, r32 = h64[:nh, 3:7], h32[:nh, 3:7]
+    rel_r = np.abs(r32 / np.where(r64 == 0, 1e-300, r64) - 1)
+    d64, d32 = h64[:nh, 1], h32[:nh, 1]
+    out = {"steps_compared": int(m64["steps"] + nh),
+           "drag": [m64["status"]["drag"], m32["status"]["drag"]],
+           "drag_rel_err": abs(m32["status"]["drag"] / m64["status"]["drag"] - 1),
+           "lift": [m64["status"]["lift"], m32["status"]["lift"]],
+           "lift_abs_err_over_drag": abs(m32["status"]["lift"] - m64["status"]["lift"]) / abs(m64["status"]["drag"]),
+           "history_steps": int(nh),
+           "resid_history_rel_err_max": float(rel_r.max()), "resid_history_rel_err_median": float(np.median(rel_r)),
+           "drag_history_rel_err_max": float(np.max(np.abs(d32 / d64 - 1))),
+           "state_l2_err_vs_fp64": [float(x) for x in np.sqrt(((q32 - q64) ** 2).mean(axis=0)
+                                                               / np.maximum((q64 ** 2).mean(axis=0), 1e-300))],
+           "state_max_err_vs_fp64": float((np.abs(q32 - q64).max(axis=0) / scale).max())}
+    if wl["need_grad"]:
+        edges = mesh.edges()
+        ti = mesh.tags.index(wl["force_tag"])
+        x, cf64 = wall_cf(edges, m64["edge_fluxes"], ti)
+        _, cf32 = wall_cf(edges, m32["edge_fluxes"], ti)
+        out["cf_rel_l2_err"] = rel_l2(cf32, cf64)
+        out["cf_max_err_over_max_cf"] = float(np.abs(cf32 - cf64).max() / max(np.abs(cf64).max(), 1e-300))
+        out["wall_edges"] = int(len(x))
+    return out
+
+
+def run_workload(kind, args, ws, rank, local, want_cpu, cells=None):
     import ebbcfd_gb300 as E
-    from ebbcfd_gb300 import _lib, meshgen
+    from ebbcfd_gb300 import _lib
 
+    wl = WORKLOADS[kind]
     L = _lib.load()
     L.ebb_set_device(local)
     t0 = time.time()
-    gen = meshgen.wedge(args.cells, seed=0)
+    gen = make_mesh(kind, cells or wl["cells"])
     mesh = gen.to_solver_mesh()
     mesh_s = time.time() - t0
     info = mesh.info
     ncell = info.n_cells
-    m64 = measure(L, E, _lib, gen, mesh, "fp64", args, local, ws, not args.no_e2e)
+    hist_steps = args.hist_steps
+    m64 = measure(L, E, _lib, mesh, wl, "fp64", args, local, ws, not args.no_e2e, hist_steps)
     split = None
     if not args.no_split:
-        m32 = measure(L, E, _lib, gen, mesh, "split", args, local, ws, not args.no_e2e)
-        q64, q32 = m64["state"], m32["state"]
-        scale = np.maximum(np.abs(q64).max(axis=0), 1e-300)
+        m32 = measure(L, E, _lib, mesh, wl, "split", args, local, ws, not args.no_e2e, hist_steps)
         split = {"value": m32["value"], "unit": "cell-updates/s", "ms_per_step": 1e3 * m32["elapsed"] / m32["steps"],
                  "speedup_vs_fp64": m32["value"] / m64["value"], "roofline": m32["roofline"],
-                 # L2 error per component relative to the component's RMS, and the largest
-                 # pointwise error relative to the component's largest magnitude
-                 "state_l2_err_vs_fp64": [float(x) for x in np.sqrt(((q32 - q64) ** 2).mean(axis=0)
-                                                                   / np.maximum((q64 ** 2).mean(axis=0), 1e-300))],
-                 "state_max_err_vs_fp64": float((np.abs(q32 - q64).max(axis=0) / scale).max()),
-                 "steps_compared": m64["steps"] + args.warmup, "clocks": m32["clocks"], "e2e": m32["e2e"]}
+                 "error_vs_fp64": split_errors(mesh, wl, m64, m32), "clocks": m32["clocks"], "e2e": m32["e2e"]}
     cpu = None
-    if rank == 0 and not args.no_cpu:
-        cpu = cpu_baseline(gen, ncell, budget_s=args.cpu_budget)
+    if rank == 0 and want_cpu:
+        cpu = cpu_baseline(gen, kind, ncell, budget_s=args.cpu_budget)
     steps_done = m64["steps"]
-    out = {
+    stages = wl["stages"]
+    return {
         "metric": "cell-updates/s", "value": m64["value"], "unit": "cell-updates/s", "n_gpus": ws,
-        "steps": steps_done, "warmup": args.warmup, "ms_per_step": 1e3 * m64["elapsed"] / max(1, steps_done),
+        "steps": steps_done, "warmup": max(args.warmup, hist_steps), "ms_per_step": 1e3 * m64["elapsed"] / max(1, steps_done),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "wedge-M2.5-rusanov-rk2-cfl0.4", "cells": ncell, "faces": info.face_slots,
+        "config": {"workload": wl["name"], "cells": ncell, "faces": info.face_slots,
                    "interior_edges": info.n_int_edges, "boundary_edges": info.n_ghost, "precision": "plain-fp64",
-                   "l2": "inputs larger than L2 (~%d MB resident)" % (sol_bytes(info) // 2 ** 20),
+                   "integrator": wl["integrator"],
+                   "l2": "inputs larger than L2 (~%d MB resident)" % (sol_bytes(info, wl["need_grad"]) // 2 ** 20),
                    "parallelism": "replicas" if ws > 1 else "single", "mesh_s": round(mesh_s, 2),
                    "setup_s": round(m64["setup_s"], 2)},
-        "cell_stages_per_s": 2 * m64["value"], "roofline": m64["roofline"], "cpu_baseline": cpu,
-        "e2e": m64["e2e"], "gpu_launches": steps_done * 7, "clocks": m64["clocks"], "split_path": split,
+        "cell_stages_per_s": stages * m64["value"], "roofline": m64["roofline"], "cpu_baseline": cpu,
+        "e2e": m64["e2e"], "gpu_launches": steps_done * (3 * stages + 1), "clocks": m64["clocks"],
+        "split_path": split,
     }
-    return out
 
 
-def sol_bytes(info):
+def sol_bytes(info, need_grad=False):
     C, S, E, G = info.n_cells, info.face_slots, info.n_int_edges, info.n_ghost
     return 8 * (12 * (C + G) + 4 * 4 * S // 3 + 8 * (C + G) + 5 * (E + G) + 12 * S)
 
 
-def cpu_baseline(gen, ncell, budget_s=20.0, steps_max=1000):
+def cpu_baseline(gen, kind, ncell, budget_s=20.0, steps_max=1000):
     from oracle import gmsh_ref, ref
+    wl = WORKLOADS[kind]
     nthreads = ref.max_threads()
     ref.set_threads(nthreads)
-    om = ref.OracleMesh(gen.as_reader_dict(), gmsh_ref.load_config(wedge_config()))
+    om = ref.OracleMesh(gen.as_reader_dict(), gmsh_ref.load_config(wl["config"]()))
     t0 = time.perf_counter()
     om.run(1)
     t1 = time.perf_counter() - t0
@@ -279,7 +441,8 @@ def cpu_baseline(gen, ncell, budget_s=20.0, steps_max=1000):
     t = time.perf_counter() - t0
     ref.set_threads(1)
     return {"value": ncell * n / t, "unit": "cell-updates/s", "cores": nthreads, "kind": "port",
-            "sample": "%d RK2 steps of the full %d-cell wedge (after 1 untimed step)" % (n, ncell)}
+            "sample": "%d %s steps of the full %d-cell %s (after 1 untimed step)" % (n, wl["integrator"], ncell,
+                                                                                     wl["name"])}
 
 
 def mms32_config():
@@ -287,19 +450,6 @@ def mms32_config():
                        "plotIter": -1, "forceBoundary": "Freestream", "integrator": "RK2_TVD", "limited": True,
                        "CFL": 0.5, "cflAdjust": False, "initialConditions": [0.5, 0, 1, 1],
                        "boudaryConditions": [{"tag": "Freestream", "type": "dirichlet", "q": [0.5, 0, 1, 1]}]})
-
-
-def plate_config():
-    bcs = [{"tag": "Inflow", "type": "fullState", "q": [0.3, 0, 1, 1]},
-           {"tag": "Top", "type": "fullState", "q": [0.3, 0, 1, 1]},
-           {"tag": "Outflow", "type": "constP", "q": [1.0 / (1.4 * 0.09)]},
-           {"tag": "Symmetry", "type": "symmetry", "q": [0.3, 0, 1, 1]},
-           {"tag": "Wall", "type": "viscidWall", "q": [0.3, 0, 1, 1]}]
-    return json.dumps({"mesh": "plate.msh", "dt": 1e-7, "tEnd": 1e9, "flux": "roeFlux", "saveIter": -1,
-                       "plotIter": -1, "forceBoundary": "Wall", "integrator": "RK4", "limited": True, "CFL": 0.8,
-                       "cflAdjust": False, "viscosity": True,
-                       "physicalConfig": {"Pr": 0.72, "R": 1.0, "gamma": 1.4, "Re": 1e5, "L": 1.0},
-                       "initialConditions": [0.3, 0, 1, 1], "boudaryConditions": bcs})
 
 
 def run_mms32(args):
@@ -409,36 +559,84 @@ def run_wedge5000(args):
     return out
 
 
-def run_plate(args):
-    """Navier-Stokes laminar flat plate on ~4.0M mixed cells: both precision forms
-    from the same start, throughput and the split path's drag error against FP64."""
-    import ctypes as C
+def run_plate20k(args):
+    """Configuration 3 run to its end: the 4.0M-cell Navier-Stokes plate (RK4, CFL 0.8),
+    20000 steps in plain FP64 and in split precision from the same initial state, every
+    step's drag and residuals recorded.  Reports each path's throughput, the drag
+    coefficient Cd = drag / (0.5 rho U^2 L_w) (wall length L_w = 2, x in [0, 2]), the
+    wall skin friction Cf(x) per x band, the split path's error against FP64 for each,
+    and the Blasius laminar value 0.664 / sqrt(Re_x) beside Cf (the boundary layer forms
+    from the leading edge; at time t it has developed over roughly x < t)."""
     import ebbcfd_gb300 as E
-    from ebbcfd_gb300 import _lib, meshgen
-    L = _lib.load()
+    from ebbcfd_gb300 import _lib
+    _lib.load()
+    steps = args.steps if args.steps_given else 20000
     t0 = time.time()
-    gen = meshgen.flat_plate(args.cells if args.cells_given else 4_000_000)
+    gen = make_mesh("plate", args.cells if args.cells_given else 4_000_000)
     mesh = gen.to_solver_mesh()
     mesh_s = time.time() - t0
-    steps = args.steps if args.steps_given else 200
-    out = {"workload": "ns-plate-M0.3-Re1e5-roe-rk4-cfl0.8", "cells": mesh.n_cells, "mesh_s": round(mesh_s, 1),
-           "steps": steps}
-    recs = {}
+    edges = mesh.edges()
+    ti = mesh.tags.index("Wall")
+    out = {"workload": PLATE_WORKLOAD + "-full", "cells": mesh.n_cells, "steps": steps, "mesh_s": round(mesh_s, 1)}
+    res = {}
     for prec in ("fp64", "split"):
         sol = E.UfvmSolver(mesh, E.load_config(plate_config()), precision=prec)
-        sol.run(args.warmup, records=False)
-        n = C.c_int64()
-        ms = C.c_double()
-        code = L.ebb_run_timed(sol.h, steps, C.byref(n), C.byref(ms))
-        if code:
-            sol._raise(code)
-        rec = sol.run(1)
-        recs[prec] = rec[-1]
-        out[prec] = {"cell_updates_per_s": mesh.n_cells * n.value / (ms.value / 1e3), "ms_per_step": ms.value / n.value,
-                     "drag": float(rec[-1][1]), "lift": float(rec[-1][2])}
+        clocks = Clocks(0)
+        clocks.start()
+        t1 = time.perf_counter()
+        err = None
+        try:
+            rec = sol.run(steps, records=True)
+        except E.EbbError as ex:
+            err = str(ex)[:160]
+            rec = None
+        wall = time.perf_counter() - t1
+        clk = clocks.stop()
+        t_end, dt_end, it = sol.time()
+        row = {"iterations": int(it), "t": t_end, "dt": dt_end, "wall_s": wall,
+               "cell_updates_per_s": mesh.n_cells * it / wall, "clocks": clk}
+        if err:
+            row["error"] = err
+        else:
+            x, cf = wall_cf(edges, sol.edge_fluxes(), ti)
+            row["drag"] = float(rec[-1, 1])
+            row["cd"] = float(rec[-1, 1] / (0.5 * 2.0))
+            row["lift"] = float(rec[-1, 2])
+            row["resid_last"] = [float(v) for v in rec[-1, 3:7]]
+            res[prec] = {"rec": rec, "x": x, "cf": cf, "state": sol.state}
+        out[prec] = row
         sol.close()
-    out["split_speedup"] = out["split"]["cell_updates_per_s"] / out["fp64"]["cell_updates_per_s"]
-    out["split_drag_rel_err"] = abs(out["split"]["drag"] / out["fp64"]["drag"] - 1)
+    if "fp64" in res and "split" in res:
+        a, b = res["fp64"], res["split"]
+        n = min(len(a["rec"]), len(b["rec"]))
+        d64, d32 = a["rec"][:n, 1], b["rec"][:n, 1]
+        r64, r32 = a["rec"][:n, 3:7], b["rec"][:n, 3:7]
+        out["split_drag_rel_err"] = abs(b["rec"][n - 1, 1] / a["rec"][n - 1, 1] - 1)
+        out["split_cd_abs_err"] = abs(b["rec"][n - 1, 1] - a["rec"][n - 1, 1]) / (0.5 * 2.0)
+        out["split_drag_history_rel_err_max"] = float(np.max(np.abs(d32 / d64 - 1)))
+        rr = np.abs(r32 / np.where(r64 == 0, 1e-300, r64) - 1)
+        out["split_resid_history_rel_err"] = {"max": float(rr.max()), "median": float(np.median(rr)),
+                                              "at_steps": {str(k): float(rr[k - 1].max()) for k in
+                                                           (1, 10, 100, 1000, 5000, 10000, 20000) if k <= n}}
+        out["split_cf_rel_l2_err"] = rel_l2(b["cf"], a["cf"])
+        out["split_cf_max_err_over_max_cf"] = float(np.abs(b["cf"] - a["cf"]).max() / np.abs(a["cf"]).max())
+        q64, q32 = a["state"], b["state"]
+        out["split_state_l2_err"] = [float(v) for v in np.sqrt(((q32 - q64) ** 2).mean(axis=0)
+                                                               / np.maximum((q64 ** 2).mean(axis=0), 1e-300))]
+        out["split_speedup"] = out["split"]["cell_updates_per_s"] / out["fp64"]["cell_updates_per_s"]
+        bands = [0.0, 0.02, 0.05, 0.1, 0.2, 0.3, 0.5, 1.0, 1.5, 2.0]
+        table = []
+        x = a["x"]
+        for lo, hi in zip(bands[:-1], bands[1:]):
+            m = (x >= lo) & (x < hi)
+            if not m.any():
+                continue
+            xc = float(x[m].mean())
+            table.append({"x_band": [lo, hi], "edges": int(m.sum()), "cf_fp64": float(a["cf"][m].mean()),
+                          "cf_split": float(b["cf"][m].mean()),
+                          "cf_rel_err": float(abs(b["cf"][m].mean() / a["cf"][m].mean() - 1)),
+                          "cf_blasius_at_mean_x": 0.664 / np.sqrt(1e5 * xc) if xc > 0 else None})
+        out["cf_table"] = table
     return out
 
 
@@ -673,46 +871,57 @@ def run_serve(args):
 
 
 def run_reference(args, ws, rank):
-    from ebbcfd_gb300 import meshgen
+    """The reference-semantics FP64 CPU restatement (oracle/, OpenMP over all host
+    threads) on the headline workload: the same mesh generator, config, metric and
+    unit; steps bounded so that the whole run stays within a few minutes."""
     from oracle import gmsh_ref, ref
-    gen = meshgen.wedge(args.cells, seed=0)
+    kind = args.workload
+    wl = WORKLOADS[kind]
+    gen = make_mesh(kind, args.cells if args.cells_given else wl["cells"])
     nthreads = ref.max_threads()
     ref.set_threads(nthreads)
-    om = ref.OracleMesh(gen.as_reader_dict(), gmsh_ref.load_config(wedge_config()))
+    om = ref.OracleMesh(gen.as_reader_dict(), gmsh_ref.load_config(wl["config"]()))
     ncell = om.n_cells
-    om.run(args.warmup)
     t0 = time.perf_counter()
     om.run(1)
     t1 = time.perf_counter() - t0
+    # warm-up (at most the budget allows), then a bounded number of timed steps
+    nw = int(max(0, min(args.warmup - 1, args.cpu_budget / max(t1, 1e-6))))
+    if nw:
+        om.run(nw)
     n = int(max(1, min(args.steps, args.cpu_budget * 4 / max(t1, 1e-6))))
     t0 = time.perf_counter()
-    if n > 1:
-        om.run(n - 1)
-    t = time.perf_counter() - t0 + t1
+    om.run(n)
+    t = time.perf_counter() - t0
     v = ncell * n / t
     return {"impl": "reference", "metric": "cell-updates/s", "value": v, "unit": "cell-updates/s", "n_gpus": ws,
-            "steps": n, "warmup": args.warmup, "ms_per_step": 1e3 * t / n, "higher_is_better": True,
+            "steps": n, "warmup": nw + 1, "ms_per_step": 1e3 * t / n, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "wedge-M2.5-rusanov-rk2-cfl0.4", "cells": ncell, "precision": "plain-fp64"},
+            "config": {"workload": wl["name"], "cells": ncell, "precision": "plain-fp64",
+                       "integrator": wl["integrator"]},
             "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": nthreads, "kind": "port",
-                             "sample": "%d of %d requested RK2 steps of the full %d-cell wedge" % (n, args.steps,
-                                                                                                   ncell)},
+                             "sample": "%d of %d requested %s steps of the full %d-cell %s" % (
+                                 n, args.steps, wl["integrator"], ncell, wl["name"])},
             "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cells", type=int, default=1_000_000)
+    ap.add_argument("--cells", type=int, default=None, help="cells of the headline mesh")
+    ap.add_argument("--wedge-cells", type=int, default=1_000_000)
+    ap.add_argument("--hist-steps", type=int, default=100,
+                    help="recorded steps before the timed ones (warm-up and the split path's history error)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-split", action="store_true")
+    ap.add_argument("--no-wedge", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
-    ap.add_argument("--workload", default="wedge",
-                    choices=["wedge", "wedge5000", "mms32", "plate4m", "batch512", "serve"])
+    ap.add_argument("--workload", default="plate",
+                    choices=["plate", "wedge", "plate20k", "wedge5000", "mms32", "batch512", "serve"])
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--seq-stride", type=int, default=4)
     ap.add_argument("--seq-steps", type=int, default=100)
@@ -724,12 +933,12 @@ def main():
     ap.add_argument("--batch-precision", default="split", choices=["split", "fp64"])
     args = ap.parse_args()
     args.steps_given = "--steps" in sys.argv
-    args.cells_given = "--cells" in sys.argv
+    args.cells_given = args.cells is not None
     args.warmup = max(3, args.warmup)
     ws, rank, local = dist_env()
-    if args.workload != "wedge":
+    if args.workload not in WORKLOADS:
         # accuracy/throughput reports for the other configurations (not the headline line)
-        run = {"mms32": run_mms32, "plate4m": run_plate, "batch512": run_batch512, "serve": run_serve,
+        run = {"mms32": run_mms32, "plate20k": run_plate20k, "batch512": run_batch512, "serve": run_serve,
                "wedge5000": run_wedge5000}
         out = run[args.workload](args)
         print(json.dumps(out))
@@ -741,7 +950,11 @@ def main():
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
-    out = run_ours(args, ws, rank, local)
+    out = run_workload(args.workload, args, ws, rank, local, not args.no_cpu, args.cells)
+    if args.workload == "plate" and not args.no_wedge:
+        w = run_workload("wedge", args, ws, rank, local, False, args.wedge_cells)
+        out["wedge"] = {k: w[k] for k in ("value", "unit", "ms_per_step", "steps", "config", "roofline", "e2e",
+                                          "clocks", "split_path")}
     if rank == 0:
         print(json.dumps(out))
     if ws > 1:

@@ -118,6 +118,7 @@ SIGNATURES = {
     "ebb_mesh_get_info": (C.c_int, [_vp, C.POINTER(MeshInfo)]),
     "ebb_mesh_get_tag": (C.c_int, [_vp, C.c_int32, _cp, C.c_size_t]),
     "ebb_mesh_centroids": (C.c_int, [_vp, _dp]),
+    "ebb_mesh_edges": (C.c_int, [_vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), _dp, _dp, _dp]),
     "ebb_mesh_free": (None, [_vp]),
     "ebb_solver_create": (C.c_int, [_vp, C.POINTER(Config), C.c_int32, C.POINTER(_vp), _cp, C.c_size_t]),
     "ebb_solver_destroy": (None, [_vp]),
@@ -131,6 +132,7 @@ SIGNATURES = {
     "ebb_step": (C.c_int, [_vp, _dp, _dp]),
     "ebb_run": (C.c_int, [_vp, C.c_int64, C.POINTER(StepRecord), C.POINTER(C.c_int64)]),
     "ebb_get_face_states": (C.c_int, [_vp, _dp]),
+    "ebb_get_edge_fluxes": (C.c_int, [_vp, _dp]),
     "ebb_run_timed": (C.c_int, [_vp, C.c_int64, C.POINTER(C.c_int64), _dp]),
     "ebb_get_stream": (C.c_int, [_vp, C.POINTER(_vp)]),
     "ebb_profile_kernels": (C.c_int, [_vp, C.c_int32, _dp]),

@@ -523,6 +523,9 @@ int assemble(ebb_solver *s, std::vector<InstLayout> &Ls, int32_t precision, std:
         inst_mu[k] = L.mu;
     }
 
+    s->flux_ref.assign(eref.begin(), eref.end());
+    s->flux_ref.insert(s->flux_ref.end(), bref.begin(), bref.end());
+
     // ---- device allocation (one arena) ----------------------------------------
     const bool split = precision == EBB_PREC_SPLIT;
     const int64_t NQ = Ct + Gt;

@@ -741,6 +741,31 @@ int ebb_mesh_centroids(const ebb_mesh *m, double *xy)
     return EBB_OK;
 }
 
+int ebb_mesh_edges(const ebb_mesh *m, int32_t *group, int32_t *cells, double *mid, double *normal, double *len)
+{
+    if (!m) return EBB_ERR_ARG;
+    Topology t;
+    std::string e;
+    if (!build_topology(*m, t, e)) return EBB_ERR_MESH;
+    for (int64_t i = 0; i < t.E; i++) {
+        if (group) group[i] = t.e_boundary[i] ? t.e_group[i] : -1;
+        if (cells) {
+            cells[2 * i] = t.e_cell0[i];
+            cells[2 * i + 1] = t.e_cell1[i];
+        }
+        if (mid) {
+            mid[2 * i] = t.e_mx[i];
+            mid[2 * i + 1] = t.e_my[i];
+        }
+        if (normal) {
+            normal[2 * i] = t.e_nx[i];
+            normal[2 * i + 1] = t.e_ny[i];
+        }
+        if (len) len[i] = t.e_len[i];
+    }
+    return EBB_OK;
+}
+
 void ebb_mesh_free(ebb_mesh *m) { delete m; }
 
 }  // extern "C"

@@ -45,6 +45,7 @@ struct ebb_solver {
     std::vector<int32_t> perm;           // device cell -> reference cell
     std::vector<int64_t> ref_face_slot;  // reference (cell, local edge) order -> device slot index
     std::vector<int32_t> ref_nedge;      // edge count per reference cell
+    std::vector<int32_t> flux_ref;       // flux index (interior edges, then boundary) -> reference edge id
     cudaStream_t stream = nullptr;
     void *dmem = nullptr;
     size_t dbytes = 0;

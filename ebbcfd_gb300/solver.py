@@ -149,6 +149,19 @@ class Mesh:
         _check(_lib.load().ebb_mesh_centroids(self.h, _dp(xy)))
         return xy
 
+    def edges(self):
+        """The reference's edges in creation order: dict of group (boundary tag index, -1
+        interior), cells (n, 2), mid (n, 2), normal (n, 2), len (n,)."""
+        n = self.info.n_edges
+        g = np.zeros(n, dtype=np.int32)
+        c = np.zeros((n, 2), dtype=np.int32)
+        mid = np.zeros((n, 2))
+        nrm = np.zeros((n, 2))
+        ln = np.zeros(n)
+        ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))
+        _check(_lib.load().ebb_mesh_edges(self.h, ip(g), ip(c), _dp(mid), _dp(nrm), _dp(ln)))
+        return {"group": g, "cells": c, "mid": mid, "normal": nrm, "len": ln}
+
     def __del__(self):
         try:
             if self.h:
@@ -257,6 +270,12 @@ class UfvmSolver:
     def face_states(self):
         out = np.zeros((self.face_slots, 4))
         self._raise(_lib.load().ebb_get_face_states(self.h, _dp(out)))
+        return out
+
+    def edge_fluxes(self):
+        """len * flux of every edge (reference edge order) of the last residual evaluation."""
+        out = np.zeros((self.mesh.info.n_edges, 4))
+        self._raise(_lib.load().ebb_get_edge_fluxes(self.h, _dp(out)))
         return out
 
     def save_solution(self, path, t=None, dt=None):

@@ -1742,6 +1742,15 @@ void o_face_states(const OMesh *m, double *out)
     }
 }
 
+/* Edge fluxes of the last residual evaluation, len * flux per edge in edge order: the
+   terms the residual sums (solve.d:1086-1096) and computeBoundaryForces adds up for
+   the force tags (mesh.d:645-671).  out: nEdges*4 doubles. */
+void o_edge_fluxes(const OMesh *m, double *out)
+{
+    for (int i = 0; i < m->nEdges; i++)
+        for (int k = 0; k < 4; k++) out[4 * i + k] = m->edges[i].flux[k] * m->edges[i].len;
+}
+
 /* Gradient and limiter of the last residual evaluation (interior cells). */
 void o_grad_lim(const OMesh *m, double *grad, double *lim)
 {

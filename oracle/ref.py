@@ -91,6 +91,7 @@ def lib():
         L.o_ms_converge.restype = C.c_long
         L.o_face_states.argtypes = [C.c_void_p, dp]
         L.o_grad_lim.argtypes = [C.c_void_p, dp, dp]
+        L.o_edge_fluxes.argtypes = [C.c_void_p, dp]
         L.o_reconstruct.argtypes = [C.c_void_p, dp, ip]
         L.o_reconstruct.restype = C.c_int
         L.o_flux_batch.argtypes = [C.c_int, C.c_int, dp, dp, dp, dp, dp]
@@ -239,6 +240,12 @@ class OracleMesh:
         n = sum(len(e) for e in self.mesh["elements"])
         out = np.zeros((n, 4))
         lib().o_face_states(self.h, _dp(out))
+        return out
+
+    def edge_fluxes(self):
+        """len * flux of every edge (reference edge order) of the last residual evaluation."""
+        out = np.zeros((self.n_edges, 4))
+        lib().o_edge_fluxes(self.h, _dp(out))
         return out
 
     def grad_lim(self):

@@ -50,9 +50,13 @@ def test_residual_one_stage(name):
         assert abs(dtg - dto) <= 1e-14 * abs(dto)
         assert abs(rmg - rmo) <= 1e-12 * abs(rmo)
         assert rel_err(sol.face_states(), om.face_states()) <= RES_TOL
+        # len * flux per edge (reference edge order), the terms of the residual and forces
+        fg, fo = sol.edge_fluxes(), om.edge_fluxes()
+        assert rel_err(fg, fo) <= RES_TOL, (name, limit, rel_err(fg, fo))
         if name not in USES_POW:
             assert np.array_equal(Rg, Ro), (name, limit, np.abs(Rg - Ro).max())
             assert dtg == dto and rmg == rmo
+            assert np.array_equal(fg, fo)
     # determinism: same inputs, same bits
     Rg2, _, _ = sol.ufvm_solver(q, limit=True)
     Rg1, _, _ = sol.ufvm_solver(q, limit=True)

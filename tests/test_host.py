@@ -121,6 +121,28 @@ def test_gmsh_import_matches_reference_reader(path):
         assert np.allclose(xy[i], p.mean(axis=0), atol=0.5 * np.ptp(p, axis=0).max())
 
 
+@pytest.mark.parametrize("path", MESHES[:4], ids=[os.path.basename(p) for p in MESHES[:4]])
+def test_mesh_edges_match_the_oracle_edges(path):
+    """ebb_mesh_edges lists the reference's edges (mesh.d:242-313 creation order) with
+    the oracle's lengths, normals, midpoints and cell indices, and the boundary group
+    of each boundary edge."""
+    from oracle import ref
+    r = gmsh_ref.parse_gmsh(path)
+    conf = {"dt": 1e-4, "dynamicDt": True, "tEnd": 1.0, "flux": "roeFlux", "integrator": "Euler", "limited": True,
+            "lpThresh": -1, "order": 2, "CFL": 0.5, "ic": [0.5, 0, 1, 1], "localTimestep": False,
+            "multistageLimiting": True, "cflAdjust": False, "viscosity": False,
+            "physicalConfig": {"Pr": 0.7, "R": 8.3145, "Re": 1000, "L": 1},
+            "boundaries": [{"tag": t, "type": 0, "q": [0.5, 0, 1, 1]} for t in r["bTags"]], "forceBoundary": []}
+    om = ref.OracleMesh(r, conf)
+    eg = om.geometry()["edge"]
+    e = E.import_mesh(path).edges()
+    assert len(e["len"]) == om.n_edges
+    assert np.array_equal(e["len"], eg[:, 0]) and np.array_equal(e["normal"], eg[:, 1:3])
+    assert np.array_equal(e["mid"], eg[:, 3:5]) and np.array_equal(e["cells"], eg[:, 5:7].astype(np.int32))
+    assert np.array_equal(e["group"] >= 0, eg[:, 7] != 0)
+    assert set(e["group"][e["group"] >= 0]) <= set(range(len(r["bTags"])))
+
+
 def write(tmp_path, name, text):
     p = tmp_path / name
     p.write_text(text)
@@ -405,18 +427,21 @@ def test_hanging_node_polygons():
 
 def test_bench_roofline_inputs():
     """bench.py's roofline inputs: the committed ncu summaries carry DRAM traffic for
-    every stage kernel of both precision forms (scaled by cell count), and the
-    algorithmic-bytes model counts the split update's freestream-correction reads."""
+    every stage kernel of both precision forms on the wedge (scaled by cell count),
+    the FP64 kernels' FP64-pipe share, and the algorithmic-bytes model counts the split
+    update's freestream-correction reads and the viscous gradient traffic."""
     import sys
     sys.path.insert(0, ROOT)
     import bench
+    wl, cells = bench.WEDGE_WORKLOAD, 1001045
     for kern in ("k_cell", "k_flux", "k_update"):
         for prec in ("fp64", "split"):
-            t = bench.profiled_traffic(kern, prec, bench.PROFILED_CELLS)
-            assert t is not None and t["bytes"] > 1e7, (kern, prec)
-            n = bench.PROFILED_CELLS // 2
-            half = bench.profiled_traffic(kern, prec, n)
-            assert abs(half["bytes"] - t["bytes"] * n / bench.PROFILED_CELLS) <= 1.0
+            t = bench.profiled_counters(kern, prec, wl, cells)["traffic"]
+            assert t is not None and t["bytes"] > 1e7 and t["captured_cells"] == cells, (kern, prec)
+            half = bench.profiled_counters(kern, prec, wl, cells // 2)["traffic"]
+            assert abs(half["bytes"] - t["bytes"] * (cells // 2) / cells) <= 1.0
+        assert bench.profiled_counters(kern, "fp64", wl, cells)["fp64_pipe_pct"] > 50
+    assert bench.profiled_counters("k_flux", "fp64", "no-such-workload", cells)["traffic"] is None
 
     class Info:
         n_cells, face_slots, n_int_edges, n_ghost = 1000, 3000, 1480, 40
@@ -425,6 +450,22 @@ def test_bench_roofline_inputs():
     assert all(v > 0 for v in b64.values()) and b32["cell"] < b64["cell"]
     plain32 = Info.n_cells * (4 + 12 + 32 + 16 + 16) + Info.face_slots * 4 + (Info.n_int_edges + Info.n_ghost) * 20
     assert b32["update"] == plain32 + Info.n_cells * 16 + Info.face_slots * 12
+    v64 = bench.algorithmic_bytes(Info, real=8, need_grad=True)
+    assert v64["flux"] == b64["flux"] + Info.n_int_edges * 8 + (Info.n_cells + Info.n_ghost) * 64
+    assert v64["cell"] == b64["cell"] + Info.n_cells * 64
+
+
+def test_bench_wall_skin_friction():
+    """Cf per wall edge from the edge fluxes: 2 * (len F1) / len on the tagged edges,
+    sorted by x; other edges are ignored."""
+    import sys
+    sys.path.insert(0, ROOT)
+    import bench
+    edges = {"group": np.array([-1, 2, 2, 0]), "mid": np.array([[0.5, 0.1], [0.7, 0.0], [0.2, 0.0], [0.1, 0.5]]),
+             "len": np.array([1.0, 0.5, 0.25, 1.0])}
+    efl = np.array([[0, 9, 0, 0], [0, 0.01, 0, 0], [0, 0.005, 0, 0], [0, 7, 0, 0]], dtype=float)
+    x, cf = bench.wall_cf(edges, efl, 2)
+    assert np.array_equal(x, [0.2, 0.7]) and np.allclose(cf, [0.04, 0.04])
 
 
 def test_wedge_mesh_quality_and_count():
