@@ -290,6 +290,7 @@ int build_instance(const ebb_mesh *mesh, const ebb_config *cfg, InstLayout &L, s
     h.dt = cfg->dt;
     h.t = 0;
     h.cfl = cfg->cfl;
+    h.cflf = (float)h.cfl;
     h.t_end = cfg->t_end;
     h.dt_half = h.dt / 2.0;
     h.dt_sixth = h.dt / 6.0;
@@ -381,7 +382,7 @@ size_t bytes_of(const Dims &D, int32_t precision)
     total += 4 * sz<int32_t>(Gt) + rsz(2 * Gt) + rsz(Gt) + 4 * rsz(4 * Gt);
     total += sz<int32_t>(D.nforce + 1) + sz<int32_t>(n + 1);
     total += 2 * sz<double>(4 * Ct);  // host-order staging, device-order scratch
-    if (n > 1) total += sz<int32_t>(Ct) + 3 * sz<int32_t>(D.nblk) + 2 * sz<int32_t>(n + 1) + sz<double>(n);
+    if (n > 1) total += sz<int32_t>(Ct) + 3 * sz<int32_t>(D.nblk) + 2 * sz<int32_t>(n + 1) + sz<double>(n) + sz<float>(n);
     return total + 32 * 256;  // empty arrays still take one 256-byte unit each
 }
 
@@ -444,6 +445,7 @@ int assemble(ebb_solver *s, std::vector<InstLayout> &Ls, int32_t precision, std:
     std::vector<int32_t> force, force_off(n + 1, 0), cell_inst(n > 1 ? Ct : 0);
     std::vector<int32_t> blk_first, blk_end, blk_inst, inst_blk(n + 1, 0), inst_c0(n + 1, 0);
     std::vector<double> inst_mu(n);
+    std::vector<float> inst_muf(n);
     s->perm.resize(Ct);
     s->ref_face_slot.clear();
     s->ref_nedge.clear();
@@ -521,6 +523,7 @@ int assemble(ebb_solver *s, std::vector<InstLayout> &Ls, int32_t precision, std:
         }
         inst_blk[k + 1] = inst_blk[k] + nb;
         inst_mu[k] = L.mu;
+        inst_muf[k] = (float)L.mu;
     }
 
     s->flux_ref.assign(eref.begin(), eref.end());
@@ -641,6 +644,7 @@ int assemble(ebb_solver *s, std::vector<InstLayout> &Ls, int32_t precision, std:
         M.inst_blk = up(ar.take<int32_t>(n + 1), inst_blk);
         M.inst_c0 = up(ar.take<int32_t>(n + 1), inst_c0);
         M.inst_mu = up(ar.take<double>(n), inst_mu);
+        M.inst_muf = up(ar.take<float>(n), inst_muf);
     }
     s->d_stage = ar.take<double>(4 * Ct);
     s->d_tmp = ar.take<double>(4 * Ct);
@@ -665,6 +669,8 @@ int assemble(ebb_solver *s, std::vector<InstLayout> &Ls, int32_t precision, std:
     P.lp_thresh = c0.lp_thresh;
     P.pr = c0.pr;
     P.mu = Ls[0].mu;
+    P.prf = (float)P.pr;
+    P.muf = (float)P.mu;
     P.r_gas = c0.r_gas;
     P.need_grad = (c0.viscosity || visc_wall) ? 1 : 0;
     std::vector<DState> st(n);

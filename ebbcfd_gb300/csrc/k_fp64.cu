@@ -65,6 +65,7 @@ template <typename T> __global__ void __launch_bounds__(EBB_RED_THREADS) k_step_
             st->resid_inc--;
         if (st->resid_inc >= 2000) {
             st->cfl *= 0.99;
+            st->cflf = (float)st->cfl;
             st->resid_inc = 0;
         }
     }

@@ -67,6 +67,21 @@ constexpr int UPD_THREADS = 256;
 #endif
 
 
+// Viscosity, Prandtl and CFL numbers in the arithmetic type: the split kernels read
+// FP32 copies rounded once on the host or in the step epilogue (a per-thread FP64
+// conversion occupies the FP64 pipe as long as an FP64 add)
+template <typename T> __device__ __forceinline__ T visc_mu(const DMesh &M, const DPhys &P, int inst);
+template <> __device__ __forceinline__ double visc_mu<double>(const DMesh &M, const DPhys &P, int inst)
+{
+    return M.inst_mu ? M.inst_mu[inst] : P.mu;
+}
+template <> __device__ __forceinline__ float visc_mu<float>(const DMesh &M, const DPhys &P, int inst)
+{
+    return M.inst_muf ? M.inst_muf[inst] : P.muf;
+}
+template <typename T> __device__ __forceinline__ T prandtl(const DPhys &P) { return sizeof(T) == 4 ? (T)P.prf : (T)P.pr; }
+template <typename T> __device__ __forceinline__ T cfl_of(const DState *st) { return sizeof(T) == 4 ? (T)st->cflf : (T)st->cfl; }
+
 __device__ __forceinline__ bool halted(const DState *st) { return st->done || st->err_key != EBB_NOERR; }
 
 __device__ __forceinline__ void flag_error(DState *st, unsigned phase, unsigned code, unsigned idx)
@@ -615,7 +630,7 @@ __device__ void boundary_flux(const DMesh &M, const DPhys &P, const DArrays &A, 
     const int inst = M.cell_inst ? M.cell_inst[owner] : 0;
     DState *st = A.st + inst;
     if (halted(st)) return;
-    const T pr = (T)P.pr, mu = (T)(M.inst_mu ? M.inst_mu[inst] : P.mu);
+    const T pr = prandtl<T>(P), mu = visc_mu<T>(M, P, inst);
     switch (type & 0xff) {
     case BC_DIRICHLET:
     case BC_FULLSTATE: {
@@ -784,7 +799,7 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? EBB_FLUX_MINB_F : EBB_FL
             dq[k][0] = T(0.5) * (g1[k][0] + g2[k][0]);
             dq[k][1] = T(0.5) * (g1[k][1] + g2[k][1]);
         }
-        diffusive_flux((T)P.pr, (T)(M.inst_mu ? M.inst_mu[inst] : P.mu), qa, dq, n.x, n.y, Fv);
+        diffusive_flux(prandtl<T>(P), visc_mu<T>(M, P, inst), qa, dq, n.x, n.y, Fv);
         for (int k = 0; k < 4; k++) F[k] = F[k] - Fv[k];
     }
     if (has_nan(F)) flag_error(st, 2, ERR_NAN_EDGE, (unsigned)M.e_ref[e]);
@@ -948,7 +963,7 @@ __global__ void __launch_bounds__(UPD_THREADS, sizeof(T) == 4 ? EBB_UPD_MINB_F :
         T *cdt = reinterpret_cast<T *>(A.cdt);
         if (need_dt || (P.local_ts && dt_update)) {
             sAve /= ld1<T>(M.g.perim, i);
-            T c = ((T)st->cfl * ld1<T>(M.g.dlen, i)) / sAve;
+            T c = (cfl_of<T>(st) * ld1<T>(M.g.dlen, i)) / sAve;
             if (need_dt) {
                 if (SPLIT)
                     fdtc = (float)c;

@@ -53,12 +53,15 @@ struct DMesh {
     const int32_t *inst_blk;           // n_inst+1 k_update block offsets
     const int32_t *force_off;          // n_inst+1 offsets into force_b
     const double *inst_mu;             // viscosity per instance
+    const float *inst_muf;             // its FP32 rounding (split path)
 };
 
 struct DPhys {
     int32_t flux, limited, order, viscous, mms, local_ts, lp;
     double lp_thresh, pr, mu, r_gas;
     int32_t need_grad;  // write raw gradients (viscous terms or viscous walls)
+    float prf, muf;     // FP32 roundings of pr and mu: the split kernels read these, so no
+                        // thread spends FP64-pipe time converting the doubles
 };
 
 // device-resident scalar state of the time loop
@@ -81,6 +84,7 @@ struct DState {
     double stop_drop;                  // > 0: done once the density residual <= stop_drop * its first value
     double resid_first;                // density residual of the first iteration (< 0: not yet seen)
     double last[7];                    // drag, lift, resid[4], Rmax of the latest iteration
+    float cflf;                        // FP32 rounding of cfl (split path)
 };
 
 // record layout matches ebb_step_record
