@@ -126,6 +126,8 @@ typedef struct {
     long iterations;
     long errIndex;
     double mmsSrcScale;
+    long nFallback[2]; /* faces whose reconstruction took the negative-pressure fallback in
+                          the last residual evaluation: [0] interior, [1] boundary */
 } OMesh;
 
 /* ------------------------------------------------------------------------- */
@@ -1159,7 +1161,7 @@ static void build_gradient(OMesh *m, double (*q)[4], int i, int limit)
 }
 
 /* face reconstruction, interior form (solve.d:980-1011) */
-static void reconstruct(const OMesh *m, double (*q)[4], uint32_t ci, const double mid[2], double out[4], int bndQuirk)
+static void reconstruct(OMesh *m, double (*q)[4], uint32_t ci, const double mid[2], double out[4], int bndQuirk)
 {
     const OCell *c = &m->cells[ci];
     double dx = mid[0] - c->centroid[0];
@@ -1172,6 +1174,8 @@ static void reconstruct(const OMesh *m, double (*q)[4], uint32_t ci, const doubl
             l1 = fmin(l1, c->lim[j][1]);
         }
         if (bndQuirk) l1 = l0; /* solve.d:311,315: boundary fallback uses lim[0] in both directions */
+#pragma omp atomic
+        m->nFallback[bndQuirk ? 1 : 0]++;
         for (int j = 0; j < 4; j++) out[j] = q[ci][j] + l0 * c->grad[j][0] * dx + l1 * c->grad[j][1] * dy;
     }
 }
@@ -1181,6 +1185,7 @@ static int has_nan4(const double f[4]) { return isnan(f[0]) || isnan(f[1]) || is
 /* ufvmSolver (solve.d:322-1122).  Returns 0 or O_ERR_NAN_EDGE (m->errIndex = edge id). */
 int o_solver(OMesh *m, double (*R)[4], double (*q)[4], double *newDt, double *Rmax, int limit, int dtUpdate)
 {
+    m->nFallback[0] = m->nFallback[1] = 0;
     const ocfg *cfg = &m->cfg;
     int C = m->nInterior;
     /* ghost states (solve.d:521-689) */
@@ -1872,6 +1877,14 @@ int o_max_threads(void)
 #else
     return 1;
 #endif
+}
+
+/* Faces of the last residual evaluation that took the negative-pressure fallback
+   (solve.d:996-1009 interior, solve.d:306-318 boundary). */
+void o_fallback_counts(const OMesh *m, long *out)
+{
+    out[0] = m->nFallback[0];
+    out[1] = m->nFallback[1];
 }
 
 double o_time(const OMesh *m) { return m->t; }

@@ -92,6 +92,7 @@ def lib():
         L.o_face_states.argtypes = [C.c_void_p, dp]
         L.o_grad_lim.argtypes = [C.c_void_p, dp, dp]
         L.o_edge_fluxes.argtypes = [C.c_void_p, dp]
+        L.o_fallback_counts.argtypes = [C.c_void_p, C.POINTER(C.c_long)]
         L.o_reconstruct.argtypes = [C.c_void_p, dp, ip]
         L.o_reconstruct.restype = C.c_int
         L.o_flux_batch.argtypes = [C.c_int, C.c_int, dp, dp, dp, dp, dp]
@@ -247,6 +248,13 @@ class OracleMesh:
         out = np.zeros((self.n_edges, 4))
         lib().o_edge_fluxes(self.h, _dp(out))
         return out
+
+    def fallback_counts(self):
+        """(interior, boundary) faces whose reconstruction took the negative-pressure
+        fallback in the last residual evaluation."""
+        out = (C.c_long * 2)()
+        lib().o_fallback_counts(self.h, out)
+        return int(out[0]), int(out[1])
 
     def grad_lim(self):
         g = np.zeros((self.n_cells, 4, 2))

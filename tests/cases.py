@@ -77,6 +77,15 @@ def all_cases():
                  {"tag": "Outflow", "type": "constP", "q": [7.936507936507937]},
                  {"tag": "Symmetry", "type": "symmetry", "q": [0.3, 0, 1, 1]},
                  {"tag": "Wall", "type": "viscidWall", "q": [0.3, 0, 1, 1]}]
+    # total temperature / total pressure inflow (solve.d:625-689, flux solve.d:939) for a
+    # Mach 0.5 stream with R = 1: T = p / rho = 1 / (1.4 * 0.25), Tt = T (1 + 0.2 M^2),
+    # Pt = p (Tt / T)^3.5.  The inflow direction is 180 degrees: solve.d:641-647 dots it
+    # with the boundary edge's outward normal, and only an inflow direction against that
+    # normal (d = +1 at the left inlet) gives the quadratic a non-negative Mach root
+    t_inf = 1.0 / (1.4 * 0.25)
+    tp_bcs = [{"tag": "Inflow", "type": "tpInflow", "q": [t_inf * 1.05, t_inf * 1.05 ** 3.5, 180.0]},
+              {"tag": "Outflow", "type": "fullState", "q": [0.5, 0, 1, 1]},
+              {"tag": "Wall", "type": "inviscidWall", "q": [0.5, 0, 1, 1]}]
     sym_visc = dict(json.loads(fp))
     return [
         Case("mms_quads_lp", "ms_refine_3.msh", text=mms_text("ms_refine_3.json"), mms=1),
@@ -103,6 +112,9 @@ def all_cases():
              text=cfg_json(initialConditions=[0.5, 0, 1, 1], integrator="RK2",
                            boudaryConditions=[{"tag": "Freestream", "type": "dirichlet", "q": [0.5, 0, 1, 1]}],
                            CFL=0.5), mms=2),
+        Case("bump_tpinflow_roe", gen=lambda: meshgen.bump_channel(3000, h=0.05, seed=2),
+             text=cfg_json(initialConditions=[0.5, 0, 1, 1], boudaryConditions=tp_bcs, integrator="RK2",
+                           physicalConfig={"Pr": 0.72, "R": 1.0, "gamma": 1.4, "Re": 1000, "L": 1.0})),
         Case("order1_local_dt", "ms_refine_tri_1.msh",
              text=mms_text("ms_refine_3.json", order=1, localTimestep=True, lpThresh=-1), mms=1),
     ]
