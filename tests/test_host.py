@@ -548,3 +548,56 @@ def test_shared_reciprocal_division_is_ieee(tmp_path):
     n, fast, bad = (int(x) for x in subprocess.run([str(exe), "4000000"], capture_output=True, text=True,
                                                    check=True).stdout.split()[-3:])
     assert n == 4000000 and fast > 0.9 * n and bad == 0
+
+
+def _c_struct_fields(text, name):
+    """Field names, in order, of `typedef struct [tag] { ... } name;` in C source."""
+    import re
+    m = re.search(r"typedef struct(?: \w+)? \{([^}]*)\} " + name + r";", text)
+    return _field_names(m.group(1))
+
+
+def _d_struct_fields(text, name):
+    import re
+    m = re.search(r"struct " + name + r"\s*\{([^}]*)\}", text)
+    return _field_names(m.group(1))
+
+
+def _field_names(body):
+    import re
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    body = re.sub(r"//[^\n]*", "", body)
+    names = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        decl = re.sub(r"\[[^\]]*\]", "", decl)  # array extents (C after the name, D after the type)
+        parts = [p.strip() for p in decl.split(",")]
+        names.append(parts[0].split()[-1])
+        names.extend(p.split()[-1] for p in parts[1:])
+    return names
+
+
+def test_d_binding_mirrors_the_header():
+    """ebbcfd_gb300/d/ebb/gb300.d (the D host's extern(C) binding) declares every
+    function of include/ebb_gb300.h with the same number of parameters, and every
+    public struct with the header's fields in the header's order."""
+    import re
+    hdr = open(os.path.join(ROOT, "include", "ebb_gb300.h")).read()
+    dsrc = open(os.path.join(ROOT, "ebbcfd_gb300", "d", "ebb", "gb300.d")).read()
+    h = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
+    d = re.sub(r"//[^\n]*", "", re.sub(r"/\+.*?\+/", "", dsrc, flags=re.S))
+
+    def protos(text):
+        out = {}
+        for m in re.finditer(r"\b(?:int|void)\s+(ebb_\w+)\s*\(([^;]*?)\)\s*;", text, flags=re.S):
+            args = m.group(2).strip()
+            out[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
+        return out
+
+    ph, pd = protos(h), protos(d)
+    assert len(ph) >= 50 and ph == pd, set(ph.items()) ^ set(pd.items())
+    for name in ("ebb_config", "ebb_boundary", "ebb_mesh_info", "ebb_step_record", "ebb_instance_status",
+                 "ebb_server_options", "ebb_request_result", "ebb_server_stats"):
+        assert _c_struct_fields(hdr, name) == _d_struct_fields(dsrc, name), name
