@@ -80,7 +80,7 @@ class ServerOptions(C.Structure):
     _fields_ = [("precision", C.c_int32), ("max_arenas", C.c_int32), ("max_batch", C.c_int32),
                 ("build_threads", C.c_int32), ("tick_ms", C.c_double), ("size_ratio", C.c_double),
                 ("arena_cells", C.c_int64), ("hbm_budget", C.c_uint64), ("escalate", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("finish_fp64", C.c_int32), ("stall_steps", C.c_int32)]
 
 
 class RequestResult(C.Structure):
@@ -88,7 +88,8 @@ class RequestResult(C.Structure):
                 ("n_cells", C.c_int64), ("iterations", C.c_int64), ("t", C.c_double), ("drag", C.c_double),
                 ("lift", C.c_double), ("resid", C.c_double * 4), ("resid_first", C.c_double),
                 ("submit_s", C.c_double), ("admit_s", C.c_double), ("finish_s", C.c_double),
-                ("precision", C.c_int32), ("escalated", C.c_int32), ("msg", C.c_char * 96)]
+                ("precision", C.c_int32), ("escalated", C.c_int32), ("split_iterations", C.c_int64),
+                ("msg", C.c_char * 96)]
 
 
 class ServerStats(C.Structure):

@@ -301,6 +301,9 @@ int build_instance(const ebb_mesh *mesh, const ebb_config *cfg, InstLayout &L, s
     h.rmax_bits = 0;
     h.err_key = EBB_NOERR;
     h.resid_last = INFINITY;
+    h.stall_steps = 0;
+    h.resid_min = INFINITY;
+    h.resid_min_iter = 0;
     h.resid_inc = 0;
     h.done = !(h.t < h.t_end);
     h.iter = 0;

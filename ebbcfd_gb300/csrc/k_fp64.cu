@@ -71,6 +71,10 @@ template <typename T> __global__ void __launch_bounds__(EBB_RED_THREADS) k_step_
     }
     st->resid_last = residMax;
     if (st->resid_first < 0) st->resid_first = resid[0];
+    if (resid[0] < st->resid_min) {
+        st->resid_min = resid[0];
+        st->resid_min_iter = st->iter;
+    }
     st->last[0] = drag;
     st->last[1] = lift;
     for (int k = 0; k < 4; k++) st->last[2 + k] = resid[k];
@@ -89,7 +93,8 @@ template <typename T> __global__ void __launch_bounds__(EBB_RED_THREADS) k_step_
     st->t += st->dt;
     st->iter++;
     st->done = !(st->t < st->t_end) || (st->max_steps > 0 && st->iter >= st->max_steps) ||
-               (st->stop_drop > 0 && resid[0] <= st->stop_drop * st->resid_first);
+               (st->stop_drop > 0 && resid[0] <= st->stop_drop * st->resid_first) ||
+               (st->stall_steps > 0 && st->iter - st->resid_min_iter > st->stall_steps);
     st->dt_half = st->dt / 2.0;
     st->dt_sixth = st->dt / 6.0;
     st->dtf = (float)st->dt;

@@ -10,7 +10,12 @@
 // physics whose cell counts are within size_ratio of its own, as long as the arena's
 // exact device bytes fit what the budget has left.  With escalation on, a request
 // whose split-precision solve stops with an error is solved again from its initial
-// state in plain FP64 (same id; the result says so).
+// state in plain FP64 (same id; the result says so).  With FP64 finishing on (the
+// default), a split-precision solve with a residual drop whose density residual has
+// levelled off -- no new minimum for stall_steps iterations: its increments are down
+// to the FP32 rounding of the flux arithmetic -- continues in plain FP64 from its
+// current state, keeping its iteration count, time and first-iteration residual, so
+// that it retires at the residual drop like an FP64 solve.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -35,7 +40,12 @@ struct Request {
     double resid_drop = 0;
     double submit_s = 0, admit_s = -1;
     int32_t precision = EBB_PREC_SPLIT;
-    int32_t escalated = 0;  // re-solved in plain FP64 after a split-precision error
+    int32_t escalated = 0;  // 1: re-solved in FP64 after a split-precision error; 2: finished in FP64
+    int64_t split_iterations = 0;
+    // a continuation starts from this state (reference cell order) and time-loop state
+    std::vector<double> resume_q;
+    ebb_instance_status resume{};
+    bool resuming = false;
     InstLayout L;
     int status = EBB_OK;
     std::string err;
@@ -106,11 +116,34 @@ void worker(ebb_server *sv)
             sv->building++;
         }
         r->status = build_instance(r->mesh.get(), &r->cfg, r->L, r->err);
-        // the mesh is kept only while an FP64 re-solve may still need it
-        if (!(sv->opt.escalate && r->precision == EBB_PREC_SPLIT)) r->mesh.reset();
+        const bool finishing = sv->opt.finish_fp64 && r->resid_drop > 0 && sv->opt.stall_steps > 0;
+        // the mesh is kept only while an FP64 re-solve or continuation may still need it
+        if (!((sv->opt.escalate || finishing) && r->precision == EBB_PREC_SPLIT)) r->mesh.reset();
         if (r->status == EBB_OK) {
             r->L.st0.max_steps = r->max_steps;
             r->L.st0.stop_drop = r->resid_drop;
+            if (finishing && r->precision == EBB_PREC_SPLIT) r->L.st0.stall_steps = sv->opt.stall_steps;
+            if (r->resuming) {
+                // continue the stopped split solve: its state (local device order) and
+                // the time-loop quantities the stop conditions and the records use
+                DState &h = r->L.st0;
+                for (int64_t i = 0; i < r->L.C; i++)
+                    for (int c = 0; c < 4; c++) r->L.q[4 * i + c] = r->resume_q[4 * (size_t)r->L.perm[i] + c];
+                h.t = r->resume.t;
+                h.dt = r->resume.dt;
+                h.dt_half = h.dt / 2.0;
+                h.dt_sixth = h.dt / 6.0;
+                h.dtf = (float)h.dt;
+                h.dt_half_f = (float)h.dt_half;
+                h.dt_sixth_f = (float)h.dt_sixth;
+                h.cfl = r->resume.cfl;
+                h.cflf = (float)h.cfl;
+                h.iter = r->resume.iterations;
+                h.resid_first = r->resume.resid_first;
+                h.done = !(h.t < h.t_end) || (h.max_steps > 0 && h.iter >= h.max_steps);
+                r->resume_q.clear();
+                r->resume_q.shrink_to_fit();
+            }
             std::vector<InstLayout> one(1);
             one[0].C = r->L.C;  // sizes only
             one[0].G = r->L.G;
@@ -139,6 +172,7 @@ void finish(ebb_server *sv, Request &r, int status, const std::string &msg, cons
     o.n_cells = r.L.C;
     o.precision = r.precision;
     o.escalated = r.escalated;
+    o.split_iterations = r.split_iterations;
     std::snprintf(o.msg, sizeof o.msg, "%s", msg.c_str());
     if (st) {
         o.err_index = st->err_index;
@@ -225,6 +259,36 @@ int harvest(ebb_server *sv, ArenaRun &a)
         a.iter_seen[k] = st[k].iterations;
         if (!st[k].done) continue;
         Request &rq = *a.reqs[k];
+        if (rq.precision == EBB_PREC_SPLIT) rq.split_iterations = st[k].iterations;
+        const bool stalled = st[k].status == EBB_OK && st[k].t < rq.cfg.t_end &&
+                             !(rq.max_steps > 0 && st[k].iterations >= rq.max_steps) &&
+                             !(rq.resid_drop > 0 && st[k].resid[0] <= rq.resid_drop * st[k].resid_first);
+        if (stalled && sv->opt.finish_fp64 && rq.precision == EBB_PREC_SPLIT && rq.mesh) {
+            // continue in plain FP64 from the current state (same id)
+            auto next = std::make_shared<Request>();
+            next->id = rq.id;
+            next->mesh = std::move(rq.mesh);
+            next->cfg = rq.cfg;
+            next->max_steps = rq.max_steps;
+            next->resid_drop = rq.resid_drop;
+            next->submit_s = rq.submit_s;
+            next->admit_s = rq.admit_s;
+            next->precision = EBB_PREC_FP64;
+            next->escalated = 2;
+            next->split_iterations = st[k].iterations;
+            next->resume = st[k];
+            next->resuming = true;
+            next->resume_q.resize(4 * (size_t)a.cells[k]);
+            if ((r = ebb_batch_get_state(a.s, k, next->resume_q.data()))) return r;
+            {
+                std::lock_guard<std::mutex> lk(sv->mu);
+                sv->to_build.push_back(next);
+            }
+            sv->cv.notify_one();
+            a.retired[k] = 1;
+            a.left--;
+            continue;
+        }
         if (st[k].status != EBB_OK && sv->opt.escalate && rq.precision == EBB_PREC_SPLIT && rq.mesh) {
             // solve it again in plain FP64, from the start
             auto again = std::make_shared<Request>();
@@ -236,6 +300,7 @@ int harvest(ebb_server *sv, ArenaRun &a)
             again->submit_s = rq.submit_s;
             again->precision = EBB_PREC_FP64;
             again->escalated = 1;
+            again->split_iterations = rq.split_iterations;
             {
                 std::lock_guard<std::mutex> lk(sv->mu);
                 sv->to_build.push_back(again);
@@ -298,7 +363,7 @@ int admit(ebb_server *sv)
         int r = (exact > room) ? EBB_ERR_OOM : assemble(a->s, Ls, head->precision, e);
         for (size_t k = 0; k < group.size(); k++) {
             group[k]->L.C = cl[k];  // keep the size for the result record
-            group[k]->admit_s = now;
+            if (group[k]->admit_s < 0) group[k]->admit_s = now;  // a continuation keeps its first admission
         }
         if (r) {
             ebb_solver_destroy(a->s);
@@ -308,6 +373,8 @@ int admit(ebb_server *sv)
         a->reqs = group;
         a->retired.assign(group.size(), 0);
         a->iter_seen.assign(group.size(), 0);
+        for (size_t k = 0; k < group.size(); k++)
+            if (group[k]->resuming) a->iter_seen[k] = group[k]->resume.iterations;
         a->cells = cl;
         a->left = (int)group.size();
         a->bytes = a->s->dbytes;
@@ -339,6 +406,8 @@ void ebb_server_options_defaults(ebb_server_options *o)
     o->size_ratio = 4.0;
     o->arena_cells = 8 << 20;
     o->hbm_budget = 150000000000ull;
+    o->finish_fp64 = 1;
+    o->stall_steps = 1000;
 }
 
 int ebb_server_create(const ebb_server_options *o, ebb_server **out, char *err, size_t err_len)

@@ -148,7 +148,8 @@ struct ebb_server_options
     long arena_cells;
     ulong hbm_budget;
     int escalate;
-    int reserved;
+    int finish_fp64;
+    int stall_steps;
 }
 
 struct ebb_request_result
@@ -165,6 +166,7 @@ struct ebb_request_result
     double submit_s, admit_s, finish_s;
     int precision;
     int escalated;
+    long split_iterations;
     char[96] msg;
 }
 

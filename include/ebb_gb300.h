@@ -309,7 +309,13 @@ typedef struct ebb_server_options {
     uint64_t hbm_budget;   /* device bytes all arenas together may take (default 150e9) */
     int32_t escalate;      /* 1: a split-precision solve that stops with an error is solved
                               again in plain FP64 from its initial state (default 0) */
-    int32_t reserved;
+    int32_t finish_fp64;   /* 1: a split-precision solve with a residual drop whose density
+                              residual makes no new minimum for stall_steps iterations (it has
+                              levelled off at the FP32 rounding of its increments) continues in
+                              plain FP64 from its current state -- same id, iteration count,
+                              time and first-iteration residual -- until the drop, its step
+                              limit or tEnd (default 1) */
+    int32_t stall_steps;   /* default 1000 */
 } ebb_server_options;
 
 typedef struct ebb_request_result {
@@ -322,7 +328,9 @@ typedef struct ebb_request_result {
     double t, drag, lift, resid[4], resid_first;
     double submit_s, admit_s, finish_s; /* server clock: seconds since ebb_server_create */
     int32_t precision;                  /* precision form of the solve that produced the result */
-    int32_t escalated;                  /* 1: re-solved in FP64 after a split-precision error */
+    int32_t escalated;                  /* 1: re-solved in FP64 after a split-precision error;
+                                           2: finished in FP64 after its split solve stalled */
+    int64_t split_iterations;           /* iterations run in split precision */
     char msg[96];
 } ebb_request_result;
 

@@ -163,3 +163,43 @@ def test_split_error_escalates_to_fp64():
         else:
             assert got["status"] in (8, 9) and got["escalated"] == 0 and got["precision"] == 1
         sv.close()
+
+
+def _serve_all(reqs, **opts):
+    """Submit every (mesh, cfg, max_steps, resid_drop) at once; run to completion."""
+    sv = E.EbbServer("split", **opts)
+    ids = {sv.submit(m, c, n, d): k for k, (m, c, n, d) in enumerate(reqs)}
+    out = {}
+    for _ in range(1000000):
+        a, w = sv.tick()
+        for r in sv.results():
+            out[ids[r["id"]]] = (r, sv.take_state(r["id"]))
+        if len(out) == len(reqs) and a == 0 and w == 0:
+            break
+    sv.close()
+    return out
+
+
+def test_stalled_split_solve_finishes_in_fp64():
+    """A split solve asked for a 1e-8 density-residual drop levels off at the FP32
+    rounding of its increments; the server continues it in plain FP64 from its state
+    (same id, iteration count, time and first-iteration residual) and retires it at the
+    drop.  The result is the same served alone and in a mix with other requests."""
+    m = meshgen.bump_channel(1500, h=0.05, seed=11).to_solver_mesh()
+    c = bump_cfg(0.5, flux="rusanovFlux")
+    drop, cap = 1e-8, 200000
+    alone = _serve_all([(m, c, cap, drop)], tick_ms=2.0)
+    r, q = alone[0]
+    assert r["status"] == 0 and r["done_reason"] == 3, r
+    assert r["escalated"] == 2 and r["precision"] == 0
+    assert 0 < r["split_iterations"] < r["iterations"] < cap
+    assert r["resid"][0] <= drop * r["resid_first"]
+    assert r["submit_s"] <= r["admit_s"] <= r["finish_s"]
+    others = [(meshgen.bump_channel(900, h=0.08, seed=12).to_solver_mesh(), bump_cfg(0.6, flux="rusanovFlux"), 300, 0.0),
+              (meshgen.bump_channel(2000, h=0.03, seed=13).to_solver_mesh(), bump_cfg(0.4, flux="rusanovFlux"), 0, 1e-3)]
+    mix = _serve_all(others[:1] + [(m, c, cap, drop)] + others[1:], tick_ms=2.0, max_batch=2)
+    r2, q2 = mix[1]
+    assert np.array_equal(q2, q)
+    for f in ("iterations", "split_iterations", "t", "drag", "lift", "done_reason", "escalated"):
+        assert r2[f] == r[f], f
+    assert mix[0][0]["done_reason"] == 2 and mix[2][0]["done_reason"] == 3
