@@ -1,101 +1,163 @@
-"""Offline autotuner for the launch bounds of the solver kernels.
+"""Offline autotuner for the launch shape of the solver kernels.
 
-The split kernels are bound by memory latency: how many warps an SM keeps in flight
-decides their speed, and that is set at compile time by the minimum-blocks-per-SM
-argument of __launch_bounds__ (it caps registers per thread; too low a cap spills).
-The FP64 kernels are bound by the FP64 pipe; a few more warps can still fill its
-gaps, so they are tuned the same way.
-For every row of candidate settings this builds a variant of the library (under
-ebbcfd_gb300/_build/tune_<k>/, with -DEBB_*_MINB_* overrides), times each kernel of
-both precision forms with ebb_profile_kernels (CUDA events on the solver stream, best
-of three rounds) on the seeded Mach 2.5 wedge, and keeps per kernel the fastest
-setting.  The kernels are independent launches, so one build per row measures all
-six at once.  Register allocation does not change results: the FP64 kernels stay
-bitwise equal to the oracle whatever the setting.
+Two dimensions per kernel are searched: threads per block and the minimum resident
+blocks per SM requested through __launch_bounds__.  The split kernels are bound by
+memory latency, so the warps an SM keeps in flight decide their speed; the block
+size and the minimum-blocks argument (a cap on registers per thread -- too low a cap
+spills) set that at compile time.  The FP64 kernels are bound by the FP64 pipe; a few
+more warps can still fill its gaps.  k_update's block size (256 or 512) is also the
+size of the per-block reduction trees and of the batched arena's update-block map, so
+one value serves both precision forms in a build.
 
-  python -m ebbcfd_gb300.autotune [--cells N] [--out PATH]
+Every row of candidate settings is one variant of the library (under
+ebbcfd_gb300/_build/tune_<k>/, with -DEBB_* overrides; the variants compile in
+parallel).  Each variant's kernels of both precision forms are timed with
+ebb_profile_kernels (CUDA events on the solver stream, best of three rounds) on the
+headline workload -- the 4.0M-cell Navier-Stokes plate (--workload wedge: the 1.0M
+Mach 2.5 wedge) -- and per kernel the fastest setting over the rows is kept.  The
+kernels are independent launches, so one variant measures all six at once.  Register
+allocation and block size change no FP64 result bit (the kernels stay bitwise equal to
+the oracle); the update block size changes the order of the RMS residual sums only.
+
+  python -m ebbcfd_gb300.autotune [--workload plate|wedge] [--cells N] [--out PATH]
 
 writes the choice as a header (default ebbcfd_gb300/csrc/tuned.h) that kernels.cuh
-includes; needs a GPU.
+includes, with every row's timings in its comments; needs a GPU.
 """
 import argparse
 import json
 import os
 import subprocess
 import sys
+from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
-# per precision form and kernel: candidate minimum blocks per SM, one row per build
-CANDIDATES = {"split": {"cell": [6, 8, 10, 12], "flux": [10, 12, 16, 20], "update": [4, 6, 8, 8]},
-              "fp64": {"cell": [1, 5, 6, 8], "flux": [1, 5, 6, 8], "update": [1, 2, 3, 4]}}
-MACRO = {("split", "cell"): "EBB_CELL_MINB_F", ("split", "flux"): "EBB_FLUX_MINB_F",
-         ("split", "update"): "EBB_UPD_MINB_F", ("fp64", "cell"): "EBB_CELL_MINB_D",
-         ("fp64", "flux"): "EBB_FLUX_MINB_D", ("fp64", "update"): "EBB_UPD_MINB_D"}
-UNIT = {"split": "k_split.cu", "fp64": "k_fp64.cu"}
-N_ROWS = 4
+# per precision form and kernel: candidate (threads per block, minimum blocks per SM),
+# one entry per row (threads x blocks <= 2048); the update kernel's threads come from
+# UPD_TB, shared by both forms
+CANDIDATES = {
+    "split": {"cell": [(128, 8), (128, 10), (128, 6), (256, 4), (256, 3), (64, 16), (64, 12)],
+              "flux": [(128, 12), (128, 10), (128, 8), (256, 6), (256, 4), (64, 20), (64, 16)],
+              "update": [8, 6, 4, 4, 3, 8, 2]},
+    "fp64": {"cell": [(128, 5), (128, 1), (128, 6), (256, 2), (256, 3), (64, 8), (64, 10)],
+             "flux": [(128, 1), (128, 4), (128, 5), (256, 2), (256, 1), (64, 8), (64, 6)],
+             "update": [3, 1, 2, 2, 1, 4, 1]},
+}
+UPD_TB = [256, 256, 256, 512, 512, 256, 512]
+N_ROWS = len(UPD_TB)
+MACRO = {("split", "cell"): ("EBB_CELL_TB_F", "EBB_CELL_MINB_F"), ("split", "flux"): ("EBB_FLUX_TB_F", "EBB_FLUX_MINB_F"),
+         ("fp64", "cell"): ("EBB_CELL_TB_D", "EBB_CELL_MINB_D"), ("fp64", "flux"): ("EBB_FLUX_TB_D", "EBB_FLUX_MINB_D"),
+         ("split", "update"): ("EBB_UPD_TB", "EBB_UPD_MINB_F"), ("fp64", "update"): ("EBB_UPD_TB", "EBB_UPD_MINB_D")}
 
 
-def _measure(row, cells):
-    """Build variant `row` and print one JSON line of kernel times (child process)."""
+def setting(row):
+    """{precision: {kernel: (threads, min blocks)}} of candidate row `row`."""
+    out = {}
+    for p, c in CANDIDATES.items():
+        out[p] = {"cell": tuple(c["cell"][row]), "flux": tuple(c["flux"][row]), "update": (UPD_TB[row], c["update"][row])}
+        for k, (tb, mb) in out[p].items():
+            assert tb * mb <= 2048, (p, k, tb, mb)
+    return out
+
+
+def defines(row):
+    d = {}
+    for (p, k), (mt, mb) in MACRO.items():
+        tb, b = setting(row)[p][k]
+        d[mt] = tb
+        d[mb] = b
+    return ["-D%s=%d" % kv for kv in sorted(d.items())]
+
+
+def _module(row):
     sys.path.insert(0, ROOT)
     from ebbcfd_gb300 import build as B
     B.OUT = os.path.join(HERE, "_build", "tune_%d" % row)
     B.LIB = os.path.join(B.OUT, "libebbgb300.so")
     B.CLI = os.path.join(B.OUT, "ebb-solve")
-    setting = {p: {k: v[row] for k, v in c.items()} for p, c in CANDIDATES.items()}
-    for p, st in setting.items():
-        B.CU[UNIT[p]] = B.CU[UNIT[p]] + ["-D%s=%d" % (MACRO[(p, k)], v) for k, v in st.items()]
-    B.build(force=True)
+    B.RECON = os.path.join(B.OUT, "ebb-reconstruct")
+    B.DEFINES = defines(row)
+    return B
+
+
+def _build(row):
+    """Compile variant `row` (child process: the build module's paths are globals)."""
+    _module(row).build(force=True)
+
+
+def _measure(row, workload, cells):
+    """Time variant `row`'s kernels; print one JSON line (child process)."""
+    _module(row)
     import ctypes as C
     import ebbcfd_gb300 as E
-    from ebbcfd_gb300 import _lib, meshgen
-    L = _lib.load()
-    mesh = meshgen.wedge(cells, seed=0).to_solver_mesh()
-    q = [2.5, 0, 1, 1]
-    cfg = E.default_config()
-    E.set_boundaries(cfg, [("Inflow", "fullState", q), ("Top", "fullState", q), ("Symmetry", "symmetry", q),
-                           ("Ramp", "inviscidWall", q), ("Outflow", "fullState", q)])
-    cfg.flux, cfg.integrator, cfg.cfl, cfg.ic[0], cfg.t_end = 0, 1, 0.4, 2.5, 1e9
+    from ebbcfd_gb300 import _lib
+    sys.path.insert(0, ROOT)
+    import bench
+    L = _lib.load(build_if_missing=False)
+    wl = bench.WORKLOADS[workload]
+    mesh = bench.make_mesh(workload, cells or wl["cells"]).to_solver_mesh()
     us = {}
     for p in CANDIDATES:
-        s = E.UfvmSolver(mesh, cfg, p)
+        s = E.UfvmSolver(mesh, E.load_config(wl["config"]()), p)
         s.run(5, records=False)
         ms = (C.c_double * 4)()
         best = None
         for _ in range(3):
-            if L.ebb_profile_kernels(s.h, 50 if p == "split" else 5, ms):
+            if L.ebb_profile_kernels(s.h, 20 if p == "split" else 3, ms):
                 raise RuntimeError("profiling failed")
             best = list(ms) if best is None else [min(a, b) for a, b in zip(best, ms)]
         s.close()
         us[p] = {"cell": 1e3 * best[0], "flux": 1e3 * best[1], "update": 1e3 * best[2]}
-    print(json.dumps({"row": row, "setting": setting, "us": us}), flush=True)
+    print(json.dumps({"row": row, "setting": setting(row), "us": us}), flush=True)
 
 
-def tune(cells=1_000_000, out=None):
-    rows = []
-    for row in range(N_ROWS):
-        p = subprocess.run([sys.executable, "-m", "ebbcfd_gb300.autotune", "--row", str(row), "--cells", str(cells)],
-                           cwd=ROOT, capture_output=True, text=True)
+def tune(workload="plate", cells=None, out=None):
+    def child(args):
+        p = subprocess.run([sys.executable, "-m", "ebbcfd_gb300.autotune"] + args, cwd=ROOT, capture_output=True,
+                           text=True)
         if p.returncode:
-            raise RuntimeError("variant %d failed:\n%s" % (row, p.stdout + p.stderr))
-        rows.append(json.loads([ln for ln in p.stdout.splitlines() if ln.startswith("{")][-1]))
+            raise RuntimeError("%s failed:\n%s" % (args, (p.stdout + p.stderr)[-3000:]))
+        return p.stdout
+
+    with ThreadPoolExecutor(max_workers=N_ROWS) as ex:
+        list(ex.map(lambda r: child(["--build-row", str(r)]), range(N_ROWS)))
+    rows = []
+    for r in range(N_ROWS):
+        o = child(["--row", str(r), "--workload", workload] + (["--cells", str(cells)] if cells else []))
+        rows.append(json.loads([ln for ln in o.splitlines() if ln.startswith("{")][-1]))
     choice, lines = {}, []
     for prec in CANDIDATES:
         for k in ("cell", "flux", "update"):
             times = {}
             for r in rows:
-                v = r["setting"][prec][k]
+                v = tuple(r["setting"][prec][k])
                 times[v] = min(times.get(v, 1e30), r["us"][prec][k])
             choice[(prec, k)] = min(times, key=times.get)
             lines.append("// %s k_%s: " % (prec, k) +
-                         ", ".join("%d blocks %.1f us" % (v, t) for v, t in sorted(times.items())))
-    text = ["// Generated by ebbcfd_gb300/autotune.py: per-kernel device time on the %d-cell seeded" % cells,
-            "// wedge, both precision forms, for each minimum number of resident blocks per SM",
-            "// requested through __launch_bounds__ (1 = the compiler's register choice)."] + lines
-    text += ["#pragma once"]
-    for key, m in MACRO.items():
-        text += ["#ifndef %s" % m, "#define %s %d" % (m, choice[key]), "#endif"]
+                         ", ".join("%dx%d %.1f us" % (tb, b, t) for (tb, b), t in sorted(times.items())))
+    # one update block size for both forms: the one whose best total is smaller
+    upd = {}
+    for tb in sorted(set(UPD_TB)):
+        upd[tb] = sum(min(r["us"][p]["update"] for r in rows if r["setting"][p]["update"][0] == tb)
+                      for p in CANDIDATES)
+    tb_upd = min(upd, key=upd.get)
+    for p in CANDIDATES:
+        best = min((r["us"][p]["update"], tuple(r["setting"][p]["update"])) for r in rows
+                   if r["setting"][p]["update"][0] == tb_upd)
+        choice[(p, "update")] = best[1]
+    cells_txt = "%d-cell" % cells if cells else "default-size"
+    text = ["// Generated by ebbcfd_gb300/autotune.py on the %s %s workload: device time per" % (cells_txt, workload),
+            "// launch of each kernel of both precision forms for each (threads per block) x (minimum",
+            "// resident blocks per SM requested through __launch_bounds__; 1 = the compiler's",
+            "// register choice), best of three rounds of CUDA-event timing; fastest kept."] + lines
+    text += ["// update block size %d (summed best update times: %s)" %
+             (tb_upd, ", ".join("%d: %.1f us" % kv for kv in sorted(upd.items()))), "#pragma once"]
+    for (p, k), (mt, mb) in MACRO.items():
+        tb, b = choice[(p, k)]
+        if k != "update" or p == "split":
+            text += ["#ifndef %s" % mt, "#define %s %d" % (mt, tb), "#endif"]
+        text += ["#ifndef %s" % mb, "#define %s %d" % (mb, b), "#endif"]
     path = out or os.path.join(HERE, "csrc", "tuned.h")
     with open(path, "w") as f:
         f.write("\n".join(text) + "\n")
@@ -104,12 +166,16 @@ def tune(cells=1_000_000, out=None):
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
-    ap.add_argument("--cells", type=int, default=1_000_000)
+    ap.add_argument("--workload", default="plate", choices=["plate", "wedge"])
+    ap.add_argument("--cells", type=int, default=None)
     ap.add_argument("--row", type=int, default=-1)
+    ap.add_argument("--build-row", type=int, default=-1)
     ap.add_argument("--out", default=None)
     a = ap.parse_args()
-    if a.row >= 0:
-        _measure(a.row, a.cells)
+    if a.build_row >= 0:
+        _build(a.build_row)
+    elif a.row >= 0:
+        _measure(a.row, a.workload, a.cells)
     else:
-        c, rows = tune(a.cells, a.out)
+        c, rows = tune(a.workload, a.cells, a.out)
         print(json.dumps({"choice": c, "rows": rows}))

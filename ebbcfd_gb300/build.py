@@ -24,6 +24,8 @@ CU = {
     "k_split.cu": ["-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"],
     "flux_noalloc.cu": ["-fmad=false"],
 }
+# extra -D overrides of the tuned launch shapes (csrc/tuned.h), set by the autotuner's variants
+DEFINES = []
 CPP = ["solver.cpp", "arena.cpp", "server.cpp", "reconstruct.cpp", "host_mesh.cpp", "host_config.cpp", "host_io.cpp"]
 
 
@@ -63,11 +65,11 @@ def build(force=False, verbose=False):
     for f, extra in CU.items():
         obj = os.path.join(OUT, f + ".o")
         jobs.append([nvcc] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]
-                    + extra + ["-c", os.path.join(CSRC, f), "-o", obj])
+                    + extra + DEFINES + ["-c", os.path.join(CSRC, f), "-o", obj])
     for f in CPP:
         obj = os.path.join(OUT, f + ".o")
         jobs.append(["g++", "-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-fno-fast-math",
-                     "-I" + os.path.join(cuda, "include"), "-c", os.path.join(CSRC, f), "-o", obj])
+                     "-I" + os.path.join(cuda, "include")] + DEFINES + ["-c", os.path.join(CSRC, f), "-o", obj])
 
     def run(cmd):
         p = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)

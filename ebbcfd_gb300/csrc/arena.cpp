@@ -15,12 +15,13 @@
 #include <numeric>
 
 #include "solver_impl.hpp"
+#include "tuned.h"
 
 namespace ebb {
 namespace {
 
 constexpr int K = kMaxEdges;
-constexpr int UPD = 256;  // k_update threads per block
+constexpr int UPD = EBB_UPD_TB;  // k_update threads per block (the tuned value the kernels use)
 
 template <typename T> size_t sz(size_t n) { return ((n * sizeof(T)) + 255) & ~(size_t)255; }
 

@@ -39,14 +39,20 @@ constexpr int BC_FULLSTATE = 0, BC_CONSTP = 1, BC_INVWALL = 2, BC_VISCWALL = 3, 
               BC_DIRICHLET = 6;
 constexpr int BC_VERTICAL = 0x100;  // flag: reflection across a vertical edge (x1 == x2)
 constexpr int ERR_NAN_EDGE = 8, ERR_NAN_CELL = 9, ERR_BC = 11;
-constexpr int UPD_THREADS = 256;
-
-// Minimum resident blocks per SM requested through __launch_bounds__ (a register cap
-// per thread: more warps in flight, possibly some spilling).  The FP32 (split)
-// kernels are memory-latency bound and gain from it; the FP64 kernels are FP64-pipe
-// bound.  Values picked by ebbcfd_gb300/autotune.py (per-kernel event timing on
-// GB300; 1 = the compiler's own register choice).
+// Threads per block and minimum resident blocks per SM requested through
+// __launch_bounds__ (a register cap per thread: more warps in flight, possibly some
+// spilling).  The FP32 (split) kernels are memory-latency bound and gain from it; the
+// FP64 kernels are FP64-pipe bound.  Values picked by ebbcfd_gb300/autotune.py
+// (per-kernel event timing on GB300; 1 = the compiler's own register choice).
 #include "tuned.h"
+constexpr int UPD_THREADS = EBB_UPD_TB;
+static_assert(EBB_UPD_TB == 256 || EBB_UPD_TB == 512, "k_update's block reductions take 256 or 512 threads");
+template <typename T> constexpr int cell_threads() { return sizeof(T) == 4 ? EBB_CELL_TB_F : EBB_CELL_TB_D; }
+template <typename T> constexpr int flux_threads() { return sizeof(T) == 4 ? EBB_FLUX_TB_F : EBB_FLUX_TB_D; }
+// an SM holds at most 2048 threads: every (threads, minimum blocks) pair must fit
+static_assert(EBB_CELL_TB_F * EBB_CELL_MINB_F <= 2048 && EBB_CELL_TB_D * EBB_CELL_MINB_D <= 2048, "k_cell bounds");
+static_assert(EBB_FLUX_TB_F * EBB_FLUX_MINB_F <= 2048 && EBB_FLUX_TB_D * EBB_FLUX_MINB_D <= 2048, "k_flux bounds");
+static_assert(EBB_UPD_TB * EBB_UPD_MINB_F <= 2048 && EBB_UPD_TB * EBB_UPD_MINB_D <= 2048, "k_update bounds");
 #ifndef EBB_CELL_MINB_F
 #define EBB_CELL_MINB_F 12
 #endif
@@ -364,7 +370,7 @@ __device__ __forceinline__ void lp_limit(const DMesh &M, int i, int ne, const T 
 }
 
 template <typename T, int MJ, bool LP, bool UNI>
-__global__ void __launch_bounds__(128, sizeof(T) == 4 ? EBB_CELL_MINB_F : EBB_CELL_MINB_D) k_cell(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, int limit)
+__global__ void __launch_bounds__(cell_threads<T>(), sizeof(T) == 4 ? EBB_CELL_MINB_F : EBB_CELL_MINB_D) k_cell(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, int limit)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool act = i < M.C;
@@ -757,7 +763,7 @@ __device__ void boundary_flux(const DMesh &M, const DPhys &P, const DArrays &A, 
 }
 
 template <typename T>
-__global__ void __launch_bounds__(128, sizeof(T) == 4 ? EBB_FLUX_MINB_F : EBB_FLUX_MINB_D) k_flux(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, int nbi)
+__global__ void __launch_bounds__(flux_threads<T>(), sizeof(T) == 4 ? EBB_FLUX_MINB_F : EBB_FLUX_MINB_D) k_flux(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, int nbi)
 {
     if ((int)blockIdx.x >= nbi) {
         grid_dep_release();
@@ -1264,7 +1270,7 @@ inline int ret(cudaError_t e) { return e == cudaSuccess ? 0 : (int)e; }
 template <typename T>
 int launch_cell_impl(const DMesh &M, const DPhys &P, const DArrays &A, const T *qin, int limit, void *stream)
 {
-    const int TB = 128;
+    const int TB = cell_threads<T>();
     dim3 grid((M.C + TB - 1) / TB);
     if (grid.x == 0) return 0;
     cudaStream_t s = (cudaStream_t)stream;
@@ -1295,7 +1301,7 @@ int launch_cell_impl(const DMesh &M, const DPhys &P, const DArrays &A, const T *
 
 template <typename T> int launch_flux_impl(const DMesh &M, const DPhys &P, const DArrays &A, const T *qin, void *stream)
 {
-    const int TB = 128;
+    const int TB = flux_threads<T>();
     int nbi = (M.Eint + TB - 1) / TB, nbb = (M.G + TB - 1) / TB;
     if (nbi + nbb == 0) return 0;
     return ret(launch_dep(k_flux<T>, dim3(nbi + nbb), dim3(TB), (cudaStream_t)stream, M, P, A, qin, nbi));

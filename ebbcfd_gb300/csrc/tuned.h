@@ -8,6 +8,21 @@
 // fp64 k_flux: 1 blocks 710.3 us, 5 blocks 713.0 us, 6 blocks 714.6 us, 8 blocks 722.2 us
 // fp64 k_update: 1 blocks 143.5 us, 2 blocks 143.4 us, 3 blocks 143.0 us, 4 blocks 143.1 us
 #pragma once
+#ifndef EBB_CELL_TB_F
+#define EBB_CELL_TB_F 128
+#endif
+#ifndef EBB_FLUX_TB_F
+#define EBB_FLUX_TB_F 128
+#endif
+#ifndef EBB_CELL_TB_D
+#define EBB_CELL_TB_D 128
+#endif
+#ifndef EBB_FLUX_TB_D
+#define EBB_FLUX_TB_D 128
+#endif
+#ifndef EBB_UPD_TB
+#define EBB_UPD_TB 256
+#endif
 #ifndef EBB_CELL_MINB_F
 #define EBB_CELL_MINB_F 8
 #endif
