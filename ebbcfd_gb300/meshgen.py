@@ -201,6 +201,42 @@ def _poisson_points(rng, xlo, xhi, ylo, yhi, h_fn, inside, h0, rho):
     return pts[kept]
 
 
+def _graded_lattice(rng, x0, x1, ylo, yhi, h_of_y, jitter=0.08):
+    """Points of a staggered triangular lattice graded in y: rows sqrt(3)/2 h(y) apart,
+    points h(y) apart along each row (odd rows shifted by half a spacing), the row
+    ends on x = x0 and x = x1, the first row at ylo excluded (it belongs to the caller)
+    and the last row on yhi; interior points jittered by up to `jitter` h (seeded).
+    Delaunay triangles of such points are close to equilateral wherever h varies slowly
+    (no slivers), so the smallest 2 A / perimeter stays a fixed fraction of h."""
+    rows = []
+    y = ylo
+    k = 0
+    while True:
+        y_next = y + 0.5 * math.sqrt(3.0) * float(h_of_y(y))
+        if y_next >= yhi - 0.4 * 0.5 * math.sqrt(3.0) * float(h_of_y(yhi)):
+            break
+        y = y_next
+        k += 1
+        rows.append((y, k))
+    rows.append((yhi, k + 1))
+    out = []
+    for y, k in rows:
+        h = float(h_of_y(y))
+        n = max(2, int(round((x1 - x0) / h)))
+        s = (x1 - x0) / n
+        if k % 2:
+            xs = np.concatenate([[x0], x0 + (np.arange(n) + 0.5) * s, [x1]])
+        else:
+            xs = x0 + np.arange(n + 1) * s
+        ys = np.full(xs.shape, y)
+        if y < yhi:  # jitter interior points (row ends stay on the side boundaries)
+            inner = slice(1, len(xs) - 1)
+            xs[inner] += rng.uniform(-jitter, jitter, len(xs) - 2) * s
+            ys[inner] += rng.uniform(-jitter, jitter, len(xs) - 2) * s
+        out.append(np.column_stack([xs, ys]))
+    return np.vstack(out)
+
+
 def wedge(n_cells=1_000_000, seed=0, angle_deg=15.0, ramp_x=0.5):
     rng = np.random.default_rng(seed)
     ta = math.tan(math.radians(angle_deg))
@@ -335,11 +371,12 @@ def flat_plate(n_cells=4_000_000, h1=1e-4, growth=1.05, seed=0, layer_top=None):
             break
     ys = np.array(ys)
     H = ys[-1]
-    # tri region spacing graded from dx at the layer top to 4 dx at y1
+    # tri region spacing graded from dx at the layer top to 4 dx at y1; a triangular
+    # lattice of spacing h has 2 / (sqrt(3)/2 h^2) triangles per unit area
     def tri_count(dx):
         yy = np.linspace(H, y1, 400)
         h = dx * (1 + 3 * (yy - H) / (y1 - H))
-        return 2 * np.trapezoid((x1 - x0) / h ** 2, yy)
+        return 2 / (0.5 * math.sqrt(3.0)) * np.trapezoid((x1 - x0) / h ** 2, yy)
     lo, hi = 1e-5, 1e-1
     for _ in range(60):
         dx = math.sqrt(lo * hi)
@@ -349,10 +386,12 @@ def flat_plate(n_cells=4_000_000, h1=1e-4, growth=1.05, seed=0, layer_top=None):
         else:
             hi = dx
     dx = math.sqrt(lo * hi)
+    # columns on x0 + i dx with the plate's leading edge x = 0 on a column
+    nl_ = int(round(-x0 / dx))
+    dx = -x0 / nl_
     nx = int(round((x1 - x0) / dx))
-    xs = np.linspace(x0, x1, nx + 1)
-    if not np.any(np.isclose(xs, 0.0)):
-        xs = np.sort(np.append(xs, 0.0))
+    xs = x0 + np.arange(nx + 1) * dx
+    xs[-1] = x1
     X, Y = np.meshgrid(xs, ys)
     qnodes = np.column_stack([X.ravel(), Y.ravel()])
     ncol = len(xs)
@@ -362,17 +401,11 @@ def flat_plate(n_cells=4_000_000, h1=1e-4, growth=1.05, seed=0, layer_top=None):
     def h_fn(x, y):
         return dx * (1 + 3 * np.clip((np.asarray(y) - H) / (y1 - H), 0, 1))
 
-    # triangle region boundary points: the layer top row is shared with the quads
+    # triangle region: the layer top row is shared with the quads; above it a seeded,
+    # jittered triangular lattice graded with h_fn (its row ends form the side
+    # boundaries, its last row the top)
     top_row = qid[-1]
-    right = _polyline([(x1, H), (x1, y1)], lambda x, y: float(h_fn(x, y)))[1:]
-    topb = _polyline([(x1, y1), (x0, y1)], lambda x, y: float(h_fn(x, y)))[1:]
-    left = _polyline([(x0, y1), (x0, H)], lambda x, y: float(h_fn(x, y)))[1:-1]
-
-    def inside(x, y, margin):
-        return (x > x0 + margin) & (x < x1 - margin) & (y > H + margin) & (y < y1 - margin)
-
-    ip = _interior_points(rng, x0, x1, H, y1, h_fn, inside, dx)
-    tnodes_extra = np.vstack([right, topb, left, ip])
+    tnodes_extra = _graded_lattice(rng, x0, x1, H, y1, lambda y: h_fn(x0, y))
     nodes = np.vstack([qnodes, tnodes_extra])
     tri_set = np.concatenate([top_row, np.arange(len(qnodes), len(nodes))])
     local = nodes[tri_set]

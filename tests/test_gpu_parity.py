@@ -17,6 +17,9 @@ pytestmark = pytest.mark.gpu
 
 NAMES = [c.name for c in all_cases()]
 USES_POW = {"flatplate_ns", "plate_ns_rk4", "bump_tpinflow_roe"}  # constP / tpInflow ghosts (solve.d:570-689)
+# cases evaluated on their initial state: a perturbed inlet state leaves the tpInflow
+# Mach quadratic (solve.d:641-669) without a non-negative root
+NO_PERTURB = {"bump_tpinflow_roe"}
 RES_TOL = 1e-12
 STATE_TOL = 1e-9
 
@@ -42,7 +45,7 @@ def rel_err(a, b):
 @pytest.mark.parametrize("name", NAMES)
 def test_residual_one_stage(name):
     sol, om = case(name).build()
-    q = perturbed(om.state())
+    q = om.state() if name in NO_PERTURB else perturbed(om.state())
     for limit in (True, False):
         Ro, dto, rmo = om.residual(q, limit=limit)
         Rg, dtg, rmg = sol.ufvm_solver(q, limit=limit)
