@@ -54,9 +54,11 @@ def check(path, ref):
     sys.path.insert(0, ROOT)
     sys.path.insert(0, os.path.join(ref, "scripts", "python"))
     import EbbUtils  # the reference's reader
+    from oracle import gmsh_ref, ref as oracle_ref
     from tests.cases import case
     sln = EbbUtils.importEbbSolution(path)
-    _, om = case(CASE).build()
+    c = case(CASE)
+    om = oracle_ref.OracleMesh(c.reader_mesh(), gmsh_ref.load_config(c.text), mms=c.mms)
     om.run(STEPS)
     q = om.state()
     faces = om.face_states()

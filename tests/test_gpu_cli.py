@@ -106,3 +106,22 @@ def test_ebb_solve_reports_missing_tag(tmp_path):
     (tmp_path / "cfg.json").write_text(json.dumps(d))
     p = subprocess.run([B.CLI, "-c", "cfg.json"], cwd=tmp_path, capture_output=True, text=True, timeout=120)
     assert p.returncode == 1 and "Could not find matching boundary condition tag" in p.stdout
+
+
+def test_esln_file_is_the_one_the_reference_reader_checked(tmp_path):
+    """The library's .esln writer gives, byte for byte, the committed fixture that the
+    reference's own reader (scripts/python/EbbUtils.py:7-77, run when the fixture was
+    made by tests/golden/make_esln_fixture.py) parsed into the oracle's state, global
+    ids, edge counts and face states."""
+    import hashlib
+    import sys
+    sys.path.insert(0, os.path.join(HERE, "golden"))
+    import make_esln_fixture as F
+    chk = json.load(open(F.CHECK))
+    out = tmp_path / "again.esln"
+    F.write(str(out))
+    data = out.read_bytes()
+    assert hashlib.sha256(data).hexdigest() == chk["sha256"]
+    assert data == open(F.FIXTURE, "rb").read()
+    r = read_esln(str(out))
+    assert r["version"] == 2 and r["M"] == 4 and len(r["q"]) == chk["found"]["n_cells"]

@@ -47,7 +47,16 @@ def test_residual_one_stage(name):
     sol, om = case(name).build()
     q = om.state() if name in NO_PERTURB else perturbed(om.state())
     for limit in (True, False):
-        Ro, dto, rmo = om.residual(q, limit=limit)
+        try:
+            Ro, dto, rmo = om.residual(q, limit=limit)
+        except RuntimeError as eo:
+            # the reference stops (e.g. the unlimited reconstruction next to the tpInflow
+            # ghost state gives a NaN flux): the GPU path stops the same way
+            with pytest.raises(E.EbbError) as eg:
+                sol.ufvm_solver(q, limit=limit)
+            assert ("status %d" % eg.value.code) in str(eo) and ("index %d" % eg.value.index) in str(eo)
+            assert limit is False or name not in NO_PERTURB
+            continue
         Rg, dtg, rmg = sol.ufvm_solver(q, limit=limit)
         assert rel_err(Rg, Ro) <= RES_TOL, (name, limit, rel_err(Rg, Ro))
         assert abs(dtg - dto) <= 1e-14 * abs(dto)

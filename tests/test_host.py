@@ -601,3 +601,19 @@ def test_d_binding_mirrors_the_header():
     for name in ("ebb_config", "ebb_boundary", "ebb_mesh_info", "ebb_step_record", "ebb_instance_status",
                  "ebb_server_options", "ebb_request_result", "ebb_server_stats"):
         assert _c_struct_fields(hdr, name) == _d_struct_fields(dsrc, name), name
+
+
+def test_esln_fixture_was_read_by_the_reference_reader():
+    """tests/golden/esln: the solution file the library wrote for a parity case, with
+    what the reference's reader (EbbUtils.importEbbSolution) found in it when the
+    fixture was made: version 2, M = 4, and cell averages, global ids, edge counts and
+    edge values equal to the oracle's."""
+    import hashlib
+    import json
+    d = os.path.join(ROOT, "tests", "golden", "esln")
+    chk = json.load(open(os.path.join(d, "reader_check.json")))
+    assert hashlib.sha256(open(os.path.join(d, chk["file"]), "rb").read()).hexdigest() == chk["sha256"]
+    f = chk["found"]
+    assert f["version"] == 2 and f["M"] == 4 and f["n_cells"] > 100
+    assert all(f[k] for k in ("cell_averages_equal_oracle_state", "global_ids_in_cell_order",
+                              "edge_counts_equal_elements", "edge_values_equal_oracle_face_states"))
