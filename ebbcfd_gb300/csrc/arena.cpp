@@ -675,6 +675,12 @@ int assemble(ebb_solver *s, std::vector<InstLayout> &Ls, int32_t precision, std:
     P.mu = Ls[0].mu;
     P.prf = (float)P.pr;
     P.muf = (float)P.mu;
+    // the same IEEE double operations the viscous flux (flux.d:28-64) performs per face
+    P.gP = 1.4 / P.pr;
+    P.c43gP = (-4.0 / 3.0) + P.gP;
+    P.m1gP = -1.0 + P.gP;
+    P.p43mgP = (4.0 / 3.0) - P.gP;
+    P.omgP = 1.0 - P.gP;
     P.r_gas = c0.r_gas;
     P.need_grad = (c0.viscosity || visc_wall) ? 1 : 0;
     std::vector<DState> st(n);

@@ -37,6 +37,25 @@ template <> struct Div<double> {
     __device__ __forceinline__ double operator()(double a) const { return ebbdiv::div(a, R); }
 };
 
+// x / 2 = 0.5 x.  FP64: on the integer pipe -- for every x whose half is a normal
+// number the product is exact and is x with its exponent field lowered by one; zeros
+// are returned as they are (0.5 * +-0 = +-0).  Subnormal or tiny (biased exponent < 2),
+// infinite and NaN values take the FP64 multiply, behind a warp vote so that a warp
+// holding none issues no FP64 instruction.  FP32: the multiply.
+template <typename T> __device__ __forceinline__ T half(T x) { return T(0.5) * x; }
+template <> __device__ __forceinline__ double half<double>(double x)
+{
+    const int hi = __double2hiint(x), lo = __double2loint(x);
+    const unsigned e = ((unsigned)hi >> 20) & 0x7ffu;
+    const bool norm = e - 2u < 2045u;
+    const bool zero = ((hi & 0x7fffffff) | lo) == 0;
+    double y = norm ? __hiloint2double(hi - 0x00100000, lo) : x;
+    if (__any_sync(__activemask(), !(norm || zero))) {
+        if (!(norm || zero)) y = x * 0.5;
+    }
+    return y;
+}
+
 template <typename T> __device__ __forceinline__ T dsqrt(T x) { return sqrt(x); }
 template <> __device__ __forceinline__ float dsqrt<float>(float x) { return sqrtf(x); }
 template <typename T> __device__ __forceinline__ T dpow(T x, T y) { return pow(x, y); }
@@ -57,7 +76,7 @@ __device__ __forceinline__ bool bounded(double x) { return bexp(x) < 1023 + 60; 
 template <typename T> __device__ __forceinline__ T pressure(const T q[4])
 {
     T a = q[1] / q[0], b = q[2] / q[0];
-    return K<T>::gm1 * (q[3] - T(0.5) * q[0] * (a * a + b * b));
+    return K<T>::gm1 * (q[3] - half(q[0]) * (a * a + b * b));
 }
 
 // Sign of source/euler.d:91-94's pressure without its two divisions.  The reference
@@ -111,7 +130,7 @@ template <typename T> __device__ __forceinline__ T pressure_of(T rho, T u, T v, 
         return __fmul_rn(K<float>::gm1,
                          __fsub_rn(e, __fmul_rn(__fmul_rn(0.5f, rho), __fadd_rn(__fmul_rn(u, u), __fmul_rn(v, v)))));
     else
-        return K<T>::gm1 * (e - T(0.5) * rho * (u * u + v * v));
+        return K<T>::gm1 * (e - half(rho) * (u * u + v * v));
 }
 
 template <typename T> __device__ __forceinline__ T entropy_fix(T lam, T eps)
@@ -153,7 +172,7 @@ __device__ __forceinline__ void roe_flux(const T qL[4], const T qR[4], T nx, T n
     T vel1 = (di * vR + vL) * d1;
     T u = vel0 * nx + vel1 * ny;
     T h = (di * hR + hL) * d1;
-    T a = dsqrt(K<T>::gm1d * (h - T(0.5) * (vel0 * vel0 + vel1 * vel1)));
+    T a = dsqrt(K<T>::gm1d * (h - half(vel0 * vel0 + vel1 * vel1)));
 
     T dRV0 = rvR0 - rvL0, dRV1 = rvR1 - rvL1;
     T dRho = rhoR - rhoL;
@@ -166,10 +185,10 @@ __device__ __forceinline__ void roe_flux(const T qL[4], const T qR[4], T nx, T n
     lam3 = entropy_fix(lam3, eps);
     sMax = max4(fabs(lam1), fabs(lam2), fabs(lam3), fabs(lam3));
 
-    T s1 = T(0.5) * (lam1 + lam2);
-    T s2 = T(0.5) * (lam1 - lam2);
+    T s1 = half(lam1 + lam2);
+    T s2 = half(lam1 - lam2);
     T qq = dsqrt(vel0 * vel0 + vel1 * vel1);
-    T G1 = gm1 * (((qq * qq) / T(2.0)) * dRho - (vel0 * dRV0 + vel1 * dRV1) + dRhoE);
+    T G1 = gm1 * (half(qq * qq) * dRho - (vel0 * dRV0 + vel1 * dRV1) + dRhoE);
     T G2 = -u * dRho + (dRV0 * nx + dRV1 * ny);
     const Div<T> byA(a);
     T C1 = (G1 / (a * a)) * (s1 - lam3) + byA(G2) * s2;
@@ -182,10 +201,10 @@ __device__ __forceinline__ void roe_flux(const T qL[4], const T qR[4], T nx, T n
     T D1 = lam3 * dRV0 + C1 * vel0 + C2 * nx;
     T D2 = lam3 * dRV1 + C1 * vel1 + C2 * ny;
     T D3 = lam3 * dRhoE + C1 * h + C2 * u;
-    out[0] = T(0.5) * (fL[0] + fR[0]) - T(0.5) * D0;
-    out[1] = T(0.5) * (fL[1] + fR[1]) - T(0.5) * D1;
-    out[2] = T(0.5) * (fL[2] + fR[2]) - T(0.5) * D2;
-    out[3] = T(0.5) * (fL[3] + fR[3]) - T(0.5) * D3;
+    out[0] = half(fL[0] + fR[0]) - half(D0);
+    out[1] = half(fL[1] + fR[1]) - half(D1);
+    out[2] = half(fL[2] + fR[2]) - half(D2);
+    out[3] = half(fL[3] + fR[3]) - half(D3);
 }
 
 // source/flux.d:66-141 (Roe-type averaged speed; every wave set to sMax)
@@ -246,10 +265,10 @@ __device__ __forceinline__ void rusanov_flux(const T qL[4], const T qR[4], T nx,
     T dRho = rhoR - rhoL;
     T dRV0 = rhoR * uR - rhoL * uL, dRV1 = rhoR * vR - rhoL * vL;
     T dRhoE = qR[3] - qL[3];
-    out[0] = T(0.5) * (fL[0] + fR[0]) - T(0.5) * (sm * dRho);
-    out[1] = T(0.5) * (fL[1] + fR[1]) - T(0.5) * (sm * dRV0);
-    out[2] = T(0.5) * (fL[2] + fR[2]) - T(0.5) * (sm * dRV1);
-    out[3] = T(0.5) * (fL[3] + fR[3]) - T(0.5) * (sm * dRhoE);
+    out[0] = half(fL[0] + fR[0]) - half(sm * dRho);
+    out[1] = half(fL[1] + fR[1]) - half(sm * dRV0);
+    out[2] = half(fL[2] + fR[2]) - half(sm * dRV1);
+    out[3] = half(fL[3] + fR[3]) - half(sm * dRhoE);
 }
 
 template <typename T>
@@ -319,23 +338,36 @@ __device__ __forceinline__ void inviscid_flux(int kind, const T qL[4], const T q
 // source/flux.d:28-64.  dq[k][r] is d(q_k)/d(x_r).  The four 4x4 matrices are
 // scaled by mu/rho and applied row by row; structurally zero entries are skipped
 // (their products are signed zeros, which leave every non-zero sum unchanged).
+// The terms of flux.d:28-64 that depend on the Prandtl number only: gamma / Pr and its
+// sums with the matrix constants.  FP64: rounded once on the host (the same IEEE
+// operations as here); FP32: formed per face from the FP32 Prandtl number.
+template <typename T> struct ViscConst {
+    T gP, c43gP, m1gP, p43mgP, omgP;  // g/Pr, -4/3 + g/Pr, -1 + g/Pr, 4/3 - g/Pr, 1 - g/Pr
+};
+template <typename T> __device__ __forceinline__ ViscConst<T> visc_const_of(T Pr)
+{
+    const T gP = K<T>::g / Pr;
+    return {gP, T(-4.0 / 3.0) + gP, T(-1.0) + gP, T(4.0 / 3.0) - gP, T(1.0) - gP};
+}
+
 template <typename T>
-__device__ __forceinline__ void diffusive_flux(T Pr, T mu, const T q[4], const T dq[4][2], T nx, T ny, T out[4])
+__device__ __forceinline__ void diffusive_flux(const ViscConst<T> &vc, T mu, const T q[4], const T dq[4][2], T nx, T ny,
+                                               T out[4])
 {
     T rho = q[0];
     const Div<T> byRho(q[0]);
     T u = byRho(q[1]);
     T v = byRho(q[2]);
     T E = byRho(q[3]);
-    T gP = K<T>::g / Pr;
+    const T gP = vc.gP;
     T s = byRho(mu);
     const T c43 = T(-4.0 / 3.0), p43 = T(4.0 / 3.0), p23 = T(2.0 / 3.0), m23 = T(-2.0 / 3.0), c231 = T(2.0 / 3.0 - 1.0);
-    T tmp0 = (c43 + gP) * (u * u) + (T(-1.0) + gP) * (v * v) - gP * E;
-    T tmp1 = (T(-1.0) + gP) * (u * u) + (c43 + gP) * (v * v) - gP * E;
+    T tmp0 = vc.c43gP * (u * u) + vc.m1gP * (v * v) - gP * E;
+    T tmp1 = vc.m1gP * (u * u) + vc.c43gP * (v * v) - gP * E;
     // A00 rows (row 0 is zero)
     T a10 = s * (c43 * u), a11 = s * p43;
     T a20 = s * (-v), a22 = s * T(1);
-    T a30 = s * tmp0, a31 = s * ((p43 - gP) * u), a32 = s * ((T(1.0) - gP) * v), a33 = s * gP;
+    T a30 = s * tmp0, a31 = s * (vc.p43mgP * u), a32 = s * (vc.omgP * v), a33 = s * gP;
     // A01
     T b10 = s * (p23 * v), b12 = s * m23;
     T b20 = s * (-u), b21 = s * T(1);
@@ -347,7 +379,7 @@ __device__ __forceinline__ void diffusive_flux(T Pr, T mu, const T q[4], const T
     // A11
     T d10 = s * (-u), d11 = s * T(1);
     T d20 = s * (c43 * v), d22 = s * p43;
-    T d30 = s * tmp1, d31 = s * ((T(1.0) - gP) * u), d32 = s * ((p43 - gP) * v), d33 = s * gP;
+    T d30 = s * tmp1, d31 = s * (vc.omgP * u), d32 = s * (vc.p43mgP * v), d33 = s * gP;
     const T x0 = dq[0][0], x1 = dq[1][0], x2 = dq[2][0], x3 = dq[3][0];
     const T y0 = dq[0][1], y1 = dq[1][1], y2 = dq[2][1], y3 = dq[3][1];
     // matrix-vector products accumulate left to right from 0 (numd Matrix * Vector)

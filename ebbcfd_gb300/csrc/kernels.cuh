@@ -85,7 +85,15 @@ template <> __device__ __forceinline__ float visc_mu<float>(const DMesh &M, cons
 {
     return M.inst_muf ? M.inst_muf[inst] : P.muf;
 }
-template <typename T> __device__ __forceinline__ T prandtl(const DPhys &P) { return sizeof(T) == 4 ? (T)P.prf : (T)P.pr; }
+template <typename T> __device__ __forceinline__ ViscConst<T> visc_const(const DPhys &P);
+template <> __device__ __forceinline__ ViscConst<double> visc_const<double>(const DPhys &P)
+{
+    return {P.gP, P.c43gP, P.m1gP, P.p43mgP, P.omgP};
+}
+template <> __device__ __forceinline__ ViscConst<float> visc_const<float>(const DPhys &P)
+{
+    return visc_const_of<float>(P.prf);
+}
 template <typename T> __device__ __forceinline__ T cfl_of(const DState *st) { return sizeof(T) == 4 ? (T)st->cflf : (T)st->cfl; }
 
 __device__ __forceinline__ bool halted(const DState *st) { return st->done || st->err_key != EBB_NOERR; }
@@ -636,7 +644,8 @@ __device__ void boundary_flux(const DMesh &M, const DPhys &P, const DArrays &A, 
     const int inst = M.cell_inst ? M.cell_inst[owner] : 0;
     DState *st = A.st + inst;
     if (halted(st)) return;
-    const T pr = prandtl<T>(P), mu = visc_mu<T>(M, P, inst);
+    const ViscConst<T> pr = visc_const<T>(P);
+    const T mu = visc_mu<T>(M, P, inst);
     switch (type & 0xff) {
     case BC_DIRICHLET:
     case BC_FULLSTATE: {
@@ -648,9 +657,9 @@ __device__ void boundary_flux(const DMesh &M, const DPhys &P, const DArrays &A, 
             load_grad<T>(A.grad, owner, g1);
             load_grad<T>(A.grad, ghost, g2);
             for (int k = 0; k < 4; k++) {
-                qa[k] = T(0.5) * (qL[k] + qR[k]);
-                dq[k][0] = T(0.5) * (g1[k][0] + g2[k][0]);
-                dq[k][1] = T(0.5) * (g1[k][1] + g2[k][1]);
+                qa[k] = half(qL[k] + qR[k]);
+                dq[k][0] = half(g1[k][0] + g2[k][0]);
+                dq[k][1] = half(g1[k][1] + g2[k][1]);
             }
             diffusive_flux(pr, mu, qa, dq, nx, ny, Fv);
             for (int k = 0; k < 4; k++) F[k] = F[k] - Fv[k];
@@ -680,7 +689,7 @@ __device__ void boundary_flux(const DMesh &M, const DPhys &P, const DArrays &A, 
         if (p < 0) p = T(1.0e-12);
         T qR[4] = {qL[0], qL[1] * -1, qL[2] * -1, qL[3]};
         T qa[4], dq[4][2], Fv[4];
-        for (int k = 0; k < 4; k++) qa[k] = T(0.5) * (qL[k] + qR[k]);
+        for (int k = 0; k < 4; k++) qa[k] = half(qL[k] + qR[k]);
         qa[1] = 0.0;
         qa[2] = 0.0;
         load_grad<T>(A.grad, owner, dq);
@@ -712,7 +721,7 @@ __device__ void boundary_flux(const DMesh &M, const DPhys &P, const DArrays &A, 
         if (P.viscous) {
             T gp[4][2], qa[4], Fv[4];
             load_grad<T>(A.grad, owner, gp);
-            for (int k = 0; k < 4; k++) qa[k] = T(0.5) * (qL[k] + qR[k]);
+            for (int k = 0; k < 4; k++) qa[k] = half(qL[k] + qR[k]);
             // bGrad = gradp*nOuter + (A*gradp)*(I - 2 nOuter), solve.d:913-925
             T nO[2][2] = {{nx * nx, nx * ny}, {ny * nx, ny * ny}};
             T Am[4][4] = {{1, 0, 0, 0}, {0, 1 - nO[0][0], 0 - nO[0][1], 0}, {0, 0 - nO[1][0], 1 - nO[1][1], 0},
@@ -745,7 +754,7 @@ __device__ void boundary_flux(const DMesh &M, const DPhys &P, const DArrays &A, 
         if (P.viscous) {
             T gp[4][2], qa[4], Fv[4];
             load_grad<T>(A.grad, owner, gp);
-            for (int k = 0; k < 4; k++) qa[k] = T(0.5) * (qL[k] + qR[k]);
+            for (int k = 0; k < 4; k++) qa[k] = half(qL[k] + qR[k]);
             diffusive_flux(pr, mu, qa, gp, nx, ny, Fv);
             for (int k = 0; k < 4; k++) F[k] = F[k] - Fv[k];
         }
@@ -801,11 +810,11 @@ __global__ void __launch_bounds__(flux_threads<T>(), sizeof(T) == 4 ? EBB_FLUX_M
         load_grad<T>(A.grad, c.x, g1);
         load_grad<T>(A.grad, c.y, g2);
         for (int k = 0; k < 4; k++) {
-            qa[k] = T(0.5) * (qL[k] + qR[k]);
-            dq[k][0] = T(0.5) * (g1[k][0] + g2[k][0]);
-            dq[k][1] = T(0.5) * (g1[k][1] + g2[k][1]);
+            qa[k] = half(qL[k] + qR[k]);
+            dq[k][0] = half(g1[k][0] + g2[k][0]);
+            dq[k][1] = half(g1[k][1] + g2[k][1]);
         }
-        diffusive_flux(prandtl<T>(P), visc_mu<T>(M, P, inst), qa, dq, n.x, n.y, Fv);
+        diffusive_flux(visc_const<T>(P), visc_mu<T>(M, P, inst), qa, dq, n.x, n.y, Fv);
         for (int k = 0; k < 4; k++) F[k] = F[k] - Fv[k];
     }
     if (has_nan(F)) flag_error(st, 2, ERR_NAN_EDGE, (unsigned)M.e_ref[e]);

@@ -62,6 +62,8 @@ struct DPhys {
     int32_t need_grad;  // write raw gradients (viscous terms or viscous walls)
     float prf, muf;     // FP32 roundings of pr and mu: the split kernels read these, so no
                         // thread spends FP64-pipe time converting the doubles
+    double gP, c43gP, m1gP, p43mgP, omgP;  // 1.4/pr, -4/3 + gP, -1 + gP, 4/3 - gP, 1 - gP (FP64
+                                           // viscous flux constants, rounded once on the host)
 };
 
 // device-resident scalar state of the time loop
