@@ -87,8 +87,9 @@ struct DState {
     double resid_first;                // density residual of the first iteration (< 0: not yet seen)
     double last[7];                    // drag, lift, resid[4], Rmax of the latest iteration
     float cflf;                        // FP32 rounding of cfl (split path)
-    int64_t stall_steps;               // > 0: done once the density residual has made no new
-                                       // minimum for this many iterations (a stalled solve)
+    int64_t stall_steps;               // > 0: done once the density residual, after falling at
+                                       // least 1000-fold from its first iteration, has made no
+                                       // new minimum for this many iterations (a stalled solve)
     int64_t resid_min_iter;            // iteration of the smallest density residual so far
     double resid_min;                  // that residual
 };

@@ -12,8 +12,9 @@
 // whose split-precision solve stops with an error is solved again from its initial
 // state in plain FP64 (same id; the result says so).  With FP64 finishing on (the
 // default), a split-precision solve with a residual drop whose density residual has
-// levelled off -- no new minimum for stall_steps iterations: its increments are down
-// to the FP32 rounding of the flux arithmetic -- continues in plain FP64 from its
+// levelled off -- fallen 1000-fold from its first iteration, then no new minimum for
+// stall_steps iterations: its increments are down to the FP32 rounding of the flux
+// arithmetic -- continues in plain FP64 from its
 // current state, keeping its iteration count, time and first-iteration residual, so
 // that it retires at the residual drop like an FP64 solve.
 #include <algorithm>

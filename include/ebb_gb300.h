@@ -310,8 +310,9 @@ typedef struct ebb_server_options {
     int32_t escalate;      /* 1: a split-precision solve that stops with an error is solved
                               again in plain FP64 from its initial state (default 0) */
     int32_t finish_fp64;   /* 1: a split-precision solve with a residual drop whose density
-                              residual makes no new minimum for stall_steps iterations (it has
-                              levelled off at the FP32 rounding of its increments) continues in
+                              residual, after falling at least 1000-fold from its first
+                              iteration, makes no new minimum for stall_steps iterations (it
+                              has levelled off at the FP32 rounding of its increments) continues in
                               plain FP64 from its current state -- same id, iteration count,
                               time and first-iteration residual -- until the drop, its step
                               limit or tEnd (default 1) */
