@@ -318,7 +318,7 @@ def measure(L, E, _lib, mesh, wl, precision, args, local, ws, want_e2e, hist_ste
         e2e = {"value": ws * ncell * k_e2e / t_e2e, "unit": "cell-updates/s", "h2d_bytes_per_step": nbytes,
                "d2h_bytes_per_step": nbytes + C.sizeof(_lib.StepRecord), "steps": k_e2e}
     peak, peak_kind = peaks()
-    ab = algorithmic_bytes(info, real=8 if precision == "fp64" else 4, need_grad=wl["need_grad"])
+    ab = algorithmic_bytes(info, real=4 if precision == "split" else 8, need_grad=wl["need_grad"])
     kernels = {}
     for k in ("cell", "flux", "update"):
         sec = kern_ms[k] * 1e-3
@@ -341,6 +341,8 @@ def measure(L, E, _lib, mesh, wl, precision, args, local, ws, want_e2e, hist_ste
             "kernels": kernels, "step_end_ms": kern_ms["step_end"]}
     if precision == "fp64":
         roof["limiter"] = "FP64 pipe (ncu fp64_pipe_active_pct; GB300 runs FP64 at a small fraction of FP32)"
+    elif precision == "df":
+        roof["limiter"] = "FP32 pipe (double-float arithmetic: 8-25 FP32 instructions per operation)"
     sol.close()
     return {"value": value, "elapsed": elapsed, "steps": steps_done, "setup_s": setup_s, "roofline": roof,
             "e2e": e2e, "clocks": clk, "state": state, "hist": hist, "status": st, "edge_fluxes": efl}
@@ -400,6 +402,12 @@ def run_workload(kind, args, ws, rank, local, want_cpu, cells=None):
         split = {"value": m32["value"], "unit": "cell-updates/s", "ms_per_step": 1e3 * m32["elapsed"] / m32["steps"],
                  "speedup_vs_fp64": m32["value"] / m64["value"], "roofline": m32["roofline"],
                  "error_vs_fp64": split_errors(mesh, wl, m64, m32), "clocks": m32["clocks"], "e2e": m32["e2e"]}
+    dfl = None
+    if not args.no_df:
+        mdf = measure(L, E, _lib, mesh, wl, "df", args, local, ws, not args.no_e2e, hist_steps)
+        dfl = {"value": mdf["value"], "unit": "cell-updates/s", "ms_per_step": 1e3 * mdf["elapsed"] / mdf["steps"],
+               "speedup_vs_fp64": mdf["value"] / m64["value"], "roofline": mdf["roofline"],
+               "error_vs_fp64": split_errors(mesh, wl, m64, mdf), "clocks": mdf["clocks"], "e2e": mdf["e2e"]}
     cpu = None
     if rank == 0 and want_cpu:
         cpu = cpu_baseline(gen, kind, ncell, budget_s=args.cpu_budget)
@@ -417,7 +425,7 @@ def run_workload(kind, args, ws, rank, local, want_cpu, cells=None):
                    "setup_s": round(m64["setup_s"], 2)},
         "cell_stages_per_s": stages * m64["value"], "roofline": m64["roofline"], "cpu_baseline": cpu,
         "e2e": m64["e2e"], "gpu_launches": steps_done * (3 * stages + 1), "clocks": m64["clocks"],
-        "split_path": split,
+        "split_path": split, "df_path": dfl,
     }
 
 
@@ -579,7 +587,7 @@ def run_plate20k(args):
     ti = mesh.tags.index("Wall")
     out = {"workload": PLATE_WORKLOAD + "-full", "cells": mesh.n_cells, "steps": steps, "mesh_s": round(mesh_s, 1)}
     res = {}
-    for prec in ("fp64", "split"):
+    for prec in ("fp64", "split", "df"):
         sol = E.UfvmSolver(mesh, E.load_config(plate_config()), precision=prec)
         clocks = Clocks(0)
         clocks.start()
@@ -637,6 +645,17 @@ def run_plate20k(args):
                           "cf_rel_err": float(abs(b["cf"][m].mean() / a["cf"][m].mean() - 1)),
                           "cf_blasius_at_mean_x": 0.664 / np.sqrt(1e5 * xc) if xc > 0 else None})
         out["cf_table"] = table
+    if "fp64" in res and "df" in res:
+        a, w = res["fp64"], res["df"]
+        n = min(len(a["rec"]), len(w["rec"]))
+        rr = np.abs(w["rec"][:n, 3:7] / np.where(a["rec"][:n, 3:7] == 0, 1e-300, a["rec"][:n, 3:7]) - 1)
+        out["df_speedup"] = out["df"]["cell_updates_per_s"] / out["fp64"]["cell_updates_per_s"]
+        out["df_drag_rel_err"] = abs(w["rec"][n - 1, 1] / a["rec"][n - 1, 1] - 1)
+        out["df_drag_history_rel_err_max"] = float(np.max(np.abs(w["rec"][:n, 1] / a["rec"][:n, 1] - 1)))
+        out["df_cf_rel_l2_err"] = rel_l2(w["cf"], a["cf"])
+        out["df_resid_history_rel_err"] = {"max": float(rr.max()), "median": float(np.median(rr))}
+        out["df_state_l2_err"] = [float(v) for v in np.sqrt(((w["state"] - a["state"]) ** 2).mean(axis=0)
+                                                            / np.maximum((a["state"] ** 2).mean(axis=0), 1e-300))]
     return out
 
 
@@ -933,6 +952,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-split", action="store_true")
     ap.add_argument("--no-wedge", action="store_true")
+    ap.add_argument("--no-df", action="store_true", help="skip the double-float precision form's leg")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--workload", default="plate",
                     choices=["plate", "wedge", "plate20k", "wedge5000", "mms32", "batch512", "serve"])
@@ -969,7 +989,7 @@ def main():
     if args.workload == "plate" and not args.no_wedge:
         w = run_workload("wedge", args, ws, rank, local, False, args.wedge_cells)
         out["wedge"] = {k: w[k] for k in ("value", "unit", "ms_per_step", "steps", "config", "roofline", "e2e",
-                                          "clocks", "split_path")}
+                                          "clocks", "split_path", "df_path")}
     if rank == 0:
         print(json.dumps(out))
     if ws > 1:

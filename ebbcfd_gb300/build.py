@@ -22,6 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU = {
     "k_fp64.cu": ["-fmad=false"],
     "k_split.cu": ["-fmad=true", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"],
+    "k_df.cu": ["-fmad=true", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"],
     "flux_noalloc.cu": ["-fmad=false"],
 }
 # extra -D overrides of the tuned launch shapes (csrc/tuned.h), set by the autotuner's variants

@@ -368,13 +368,14 @@ Dims dims_of(const std::vector<InstLayout> &Ls)
 size_t bytes_of(const Dims &D, int32_t precision)
 {
     const bool split = precision == EBB_PREC_SPLIT;
-    const size_t rs = split ? sizeof(float) : sizeof(double);
+    const bool dfp = precision == EBB_PREC_DF;
+    const size_t rs = split ? sizeof(float) : sizeof(double);  // a double-float is 8 bytes too
     auto rsz = [&](size_t m) { return ((m * rs) + 255) & ~(size_t)255; };
     const int64_t NQ = D.Ct + D.Gt, MJ = D.MJ, Cs = D.Cs, Ct = D.Ct, Gt = D.Gt, Et = D.Et;
     const int n = D.n;
     size_t total = 0;
     total += sz<double>(4 * NQ);                           // q64
-    total += split ? rsz(4 * NQ) : 0;                      // qs1 (float shadow)
+    total += (split || dfp) ? rsz(4 * NQ) : 0;             // qs1 (FP32 or double-float shadow)
     total += 2 * rsz(4 * NQ);                              // qs, aux
     total += rsz(4 * MJ * Cs) + rsz(8 * NQ);               // face, grad
     total += rsz(4 * (Et + Gt)) + rsz(Et + Gt) + rsz(Ct);  // fl, fs, cdt
@@ -535,6 +536,7 @@ int assemble(ebb_solver *s, std::vector<InstLayout> &Ls, int32_t precision, std:
 
     // ---- device allocation (one arena) ----------------------------------------
     const bool split = precision == EBB_PREC_SPLIT;
+    const bool dfp = precision == EBB_PREC_DF;
     const int64_t NQ = Ct + Gt;
     const int nblk = D.nblk;
     s->nred = nblk;
@@ -551,7 +553,7 @@ int assemble(ebb_solver *s, std::vector<InstLayout> &Ls, int32_t precision, std:
     DArrays &A = s->A;
     auto takeR = [&](size_t m) -> void * { return split ? (void *)ar.take<float>(m) : (void *)ar.take<double>(m); };
     A.q64 = ar.take<double>(4 * NQ);
-    A.qs1 = split ? takeR(4 * NQ) : (void *)A.q64;
+    A.qs1 = (split || dfp) ? takeR(4 * NQ) : (void *)A.q64;
     A.qs = takeR(4 * NQ);
     A.aux = takeR(4 * NQ);
     A.face = takeR(4 * MJ * Cs);
@@ -583,6 +585,10 @@ int assemble(ebb_solver *s, std::vector<InstLayout> &Ls, int32_t precision, std:
         if (split) {
             std::vector<float> f(v.begin(), v.end());
             cudaMemcpyAsync(dst, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream);
+            cudaStreamSynchronize(s->stream);
+        } else if (dfp) {
+            std::vector<ebbdf::df> f(v.begin(), v.end());
+            cudaMemcpyAsync(dst, f.data(), f.size() * sizeof(ebbdf::df), cudaMemcpyHostToDevice, s->stream);
             cudaStreamSynchronize(s->stream);
         } else {
             cudaMemcpyAsync(dst, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, s->stream);
@@ -658,6 +664,11 @@ int assemble(ebb_solver *s, std::vector<InstLayout> &Ls, int32_t precision, std:
         cudaMemcpyAsync(A.grad, gf.data(), gf.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream);
         cudaStreamSynchronize(s->stream);
         launch_to_float4(A.q64, reinterpret_cast<float *>(A.qs1), Ct, s->stream);
+    } else if (dfp) {
+        std::vector<ebbdf::df> gw(grad.begin(), grad.end());
+        cudaMemcpyAsync(A.grad, gw.data(), gw.size() * sizeof(ebbdf::df), cudaMemcpyHostToDevice, s->stream);
+        cudaStreamSynchronize(s->stream);
+        launch_to_df4(A.q64, A.qs1, Ct, s->stream);
     } else {
         up(reinterpret_cast<double *>(A.grad), grad);
     }
@@ -681,6 +692,12 @@ int assemble(ebb_solver *s, std::vector<InstLayout> &Ls, int32_t precision, std:
     P.m1gP = -1.0 + P.gP;
     P.p43mgP = (4.0 / 3.0) - P.gP;
     P.omgP = 1.0 - P.gP;
+    P.gPw = P.gP;
+    P.c43gPw = P.c43gP;
+    P.m1gPw = P.m1gP;
+    P.p43mgPw = P.p43mgP;
+    P.omgPw = P.omgP;
+    P.muw = P.mu;
     P.r_gas = c0.r_gas;
     P.need_grad = (c0.viscosity || visc_wall) ? 1 : 0;
     std::vector<DState> st(n);

@@ -9,9 +9,18 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <type_traits>
+
+#include "dfloat.h"
 #include "fdiv.h"
 
 namespace ebbdev {
+
+using ebbdf::df;
+// the three arithmetic types: double (plain FP64), float (split), df (double-float)
+template <typename T> constexpr bool is_fp64 = std::is_same<T, double>::value;
+template <typename T> constexpr bool is_fp32 = std::is_same<T, float>::value;
+template <typename T> constexpr bool is_df = std::is_same<T, df>::value;
 
 // gamma is an immutable 1.4 (source/euler.d:89)
 template <typename T> struct K;
@@ -20,6 +29,9 @@ template <> struct K<double> {
 };
 template <> struct K<float> {
     static constexpr float g = 1.4f, gm1 = 1.4f - 1, gm1d = 1.4f - 1.0f;
+};
+template <> struct K<df> {  // the double constants, as double-floats
+    static constexpr df g = df(1.4), gm1 = df(1.4 - 1), gm1d = df(1.4 - 1.0);
 };
 
 // Quotients by one divisor.  FP64: one correctly rounded reciprocal of the divisor
@@ -60,6 +72,8 @@ template <typename T> __device__ __forceinline__ T dsqrt(T x) { return sqrt(x); 
 template <> __device__ __forceinline__ float dsqrt<float>(float x) { return sqrtf(x); }
 template <typename T> __device__ __forceinline__ T dpow(T x, T y) { return pow(x, y); }
 template <> __device__ __forceinline__ float dpow<float>(float x, float y) { return powf(x, y); }
+// double-float: the power in FP64 (constant-pressure and inflow ghost states only)
+template <> __device__ __forceinline__ df dpow<df>(df x, df y) { return df(pow((double)x, (double)y)); }
 
 // Binary exponent of |x| (biased by 1023), read on the integer pipe; 0x7ff for inf/NaN.
 __device__ __forceinline__ int bexp(double x) { return (__double2hiint(x) >> 20) & 0x7ff; }
@@ -96,6 +110,7 @@ __device__ __forceinline__ bool pressure_negative(const double q[4])
     return pressure(q) < 0;
 }
 __device__ __forceinline__ bool pressure_negative(const float q[4]) { return pressure(q) < 0; }
+__device__ __forceinline__ bool pressure_negative(const df q[4]) { return pressure(q) < df(0.0f); }
 
 // source/flux.d:19-24.  Single precision rounds every operation on its own (no
 // multiply-add contraction): the flux kernel's value for two equal face states and the
@@ -104,7 +119,7 @@ __device__ __forceinline__ bool pressure_negative(const float q[4]) { return pre
 template <typename T>
 __device__ __forceinline__ void convective_flux(T p, T u, T v, T rho, T e, T nx, T ny, T out[4])
 {
-    if constexpr (sizeof(T) == 4) {
+    if constexpr (is_fp32<T>) {
         const float ru = __fmul_rn(rho, u), rv = __fmul_rn(rho, v), ruv = __fmul_rn(ru, v), pe = __fadd_rn(p, e);
         const float f1 = __fadd_rn(p, __fmul_rn(rho, __fmul_rn(u, u))), h2 = __fadd_rn(p, __fmul_rn(rho, __fmul_rn(v, v)));
         const float f3 = __fmul_rn(u, pe), h3 = __fmul_rn(v, pe);
@@ -126,7 +141,7 @@ __device__ __forceinline__ void convective_flux(T p, T u, T v, T rho, T e, T nx,
 // single precision without contraction, as convective_flux
 template <typename T> __device__ __forceinline__ T pressure_of(T rho, T u, T v, T e)
 {
-    if constexpr (sizeof(T) == 4)
+    if constexpr (is_fp32<T>)
         return __fmul_rn(K<float>::gm1,
                          __fsub_rn(e, __fmul_rn(__fmul_rn(0.5f, rho), __fadd_rn(__fmul_rn(u, u), __fmul_rn(v, v)))));
     else
@@ -220,7 +235,7 @@ __device__ __forceinline__ void rusanov_flux_full(const T qL[4], const T qR[4], 
 template <typename T>
 __device__ __forceinline__ void rusanov_flux(const T qL[4], const T qR[4], T nx, T ny, T out[4], T &sMax)
 {
-    if (sizeof(T) == 8) {
+    if constexpr (is_fp64<T>) {
         const double *a = reinterpret_cast<const double *>(qL), *b = reinterpret_cast<const double *>(qR);
         bool ok = mid_range(a[0], true) && mid_range(b[0], true) && bounded(a[1]) && bounded(a[2]) &&
                   bounded(a[3]) && bounded(b[1]) && bounded(b[2]) && bounded(b[3]);
@@ -245,7 +260,7 @@ __device__ __forceinline__ void rusanov_flux(const T qL[4], const T qR[4], T nx,
     T u = vel0 * nx + vel1 * ny;
     T p = byS(sL * pL + sR * pR);
     T a = dsqrt(K<T>::g * (p / rho));
-    if (sizeof(T) == 8) {
+    if constexpr (is_fp64<T>) {
         const int e = bexp((double)a);
         if (!(e >= 1023 - 200 && e < 1023 + 100)) {
             rusanov_flux_full(qL, qR, nx, ny, out, sMax);

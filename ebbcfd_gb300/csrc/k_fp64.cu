@@ -5,6 +5,7 @@
 // reference's left-to-right order, so results are bitwise those of the FP64 CPU
 // path (up to the sign of exact zeros) except where CUDA's pow() is used
 // (constant-pressure ghost states).
+#include "../../include/ebb_gb300.h"
 #include "kernels.cuh"
 
 EBB_INSTANTIATE(double)
@@ -190,12 +191,14 @@ int update_blocks(int C) { return (C + UPD_THREADS - 1) / UPD_THREADS; }
 
 int update_grid(const DMesh &M) { return M.n_upd_blocks; }
 
-int launch_step_end(const DMesh &M, const DArrays &A, int nred_blocks, int split, void *stream)
+int launch_step_end(const DMesh &M, const DArrays &A, int nred_blocks, int precision, void *stream)
 {
     const int n = M.n_inst > 0 ? M.n_inst : 1;
     cudaError_t e;
-    if (split)
+    if (precision == EBB_PREC_SPLIT)
         e = launch_dep(k_step_end<float>, dim3(n), dim3(EBB_RED_THREADS), (cudaStream_t)stream, M, A, nred_blocks);
+    else if (precision == EBB_PREC_DF)
+        e = launch_dep(k_step_end<ebbdf::df>, dim3(n), dim3(EBB_RED_THREADS), (cudaStream_t)stream, M, A, nred_blocks);
     else
         e = launch_dep(k_step_end<double>, dim3(n), dim3(EBB_RED_THREADS), (cudaStream_t)stream, M, A, nred_blocks);
     return ret(e);

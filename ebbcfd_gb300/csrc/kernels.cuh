@@ -47,12 +47,38 @@ constexpr int ERR_NAN_EDGE = 8, ERR_NAN_CELL = 9, ERR_BC = 11;
 #include "tuned.h"
 constexpr int UPD_THREADS = EBB_UPD_TB;
 static_assert(EBB_UPD_TB == 256 || EBB_UPD_TB == 512, "k_update's block reductions take 256 or 512 threads");
-template <typename T> constexpr int cell_threads() { return sizeof(T) == 4 ? EBB_CELL_TB_F : EBB_CELL_TB_D; }
-template <typename T> constexpr int flux_threads() { return sizeof(T) == 4 ? EBB_FLUX_TB_F : EBB_FLUX_TB_D; }
+// launch shapes per arithmetic type: _F split (float), _D plain FP64, _W double-float
+#ifndef EBB_CELL_TB_W
+#define EBB_CELL_TB_W 128
+#endif
+#ifndef EBB_FLUX_TB_W
+#define EBB_FLUX_TB_W 128
+#endif
+#ifndef EBB_CELL_MINB_W
+#define EBB_CELL_MINB_W 2
+#endif
+#ifndef EBB_FLUX_MINB_W
+#define EBB_FLUX_MINB_W 2
+#endif
+#ifndef EBB_UPD_MINB_W
+#define EBB_UPD_MINB_W 3
+#endif
+template <typename T> constexpr int pick(int f, int d, int w)
+{
+    return std::is_same<T, float>::value ? f : (std::is_same<T, double>::value ? d : w);
+}
+template <typename T> constexpr int cell_threads() { return pick<T>(EBB_CELL_TB_F, EBB_CELL_TB_D, EBB_CELL_TB_W); }
+template <typename T> constexpr int flux_threads() { return pick<T>(EBB_FLUX_TB_F, EBB_FLUX_TB_D, EBB_FLUX_TB_W); }
+template <typename T> constexpr int cell_minb() { return pick<T>(EBB_CELL_MINB_F, EBB_CELL_MINB_D, EBB_CELL_MINB_W); }
+template <typename T> constexpr int flux_minb() { return pick<T>(EBB_FLUX_MINB_F, EBB_FLUX_MINB_D, EBB_FLUX_MINB_W); }
+template <typename T> constexpr int upd_minb() { return pick<T>(EBB_UPD_MINB_F, EBB_UPD_MINB_D, EBB_UPD_MINB_W); }
 // an SM holds at most 2048 threads: every (threads, minimum blocks) pair must fit
 static_assert(EBB_CELL_TB_F * EBB_CELL_MINB_F <= 2048 && EBB_CELL_TB_D * EBB_CELL_MINB_D <= 2048, "k_cell bounds");
 static_assert(EBB_FLUX_TB_F * EBB_FLUX_MINB_F <= 2048 && EBB_FLUX_TB_D * EBB_FLUX_MINB_D <= 2048, "k_flux bounds");
 static_assert(EBB_UPD_TB * EBB_UPD_MINB_F <= 2048 && EBB_UPD_TB * EBB_UPD_MINB_D <= 2048, "k_update bounds");
+static_assert(EBB_CELL_TB_W * EBB_CELL_MINB_W <= 2048 && EBB_FLUX_TB_W * EBB_FLUX_MINB_W <= 2048 &&
+                  EBB_UPD_TB * EBB_UPD_MINB_W <= 2048,
+              "double-float bounds");
 #ifndef EBB_CELL_MINB_F
 #define EBB_CELL_MINB_F 12
 #endif
@@ -85,6 +111,10 @@ template <> __device__ __forceinline__ float visc_mu<float>(const DMesh &M, cons
 {
     return M.inst_muf ? M.inst_muf[inst] : P.muf;
 }
+template <> __device__ __forceinline__ df visc_mu<df>(const DMesh &M, const DPhys &P, int inst)
+{
+    return M.inst_mu ? df(M.inst_mu[inst]) : P.muw;
+}
 template <typename T> __device__ __forceinline__ ViscConst<T> visc_const(const DPhys &P);
 template <> __device__ __forceinline__ ViscConst<double> visc_const<double>(const DPhys &P)
 {
@@ -94,7 +124,17 @@ template <> __device__ __forceinline__ ViscConst<float> visc_const<float>(const 
 {
     return visc_const_of<float>(P.prf);
 }
-template <typename T> __device__ __forceinline__ T cfl_of(const DState *st) { return sizeof(T) == 4 ? (T)st->cflf : (T)st->cfl; }
+template <> __device__ __forceinline__ ViscConst<df> visc_const<df>(const DPhys &P)
+{
+    return {P.gPw, P.c43gPw, P.m1gPw, P.p43mgPw, P.omgPw};
+}
+template <typename T> __device__ __forceinline__ T cfl_of(const DState *st)
+{
+    if constexpr (is_fp32<T>)
+        return st->cflf;
+    else
+        return T(st->cfl);
+}
 
 __device__ __forceinline__ bool halted(const DState *st) { return st->done || st->err_key != EBB_NOERR; }
 
@@ -171,7 +211,29 @@ __device__ __forceinline__ void st4(float *p, const float v[4])
 {
     *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
 }
+// double-floats: (hi, lo) pairs, two 16-byte accesses per 4-vector as for double
+__device__ __forceinline__ void ld4(const df *p, df v[4])
+{
+    const float4 *q = reinterpret_cast<const float4 *>(p);
+    const float4 a = q[0], b = q[1];
+    v[0] = df(a.x, a.y);
+    v[1] = df(a.z, a.w);
+    v[2] = df(b.x, b.y);
+    v[3] = df(b.z, b.w);
+}
+__device__ __forceinline__ void st4(df *p, const df v[4])
+{
+    float4 *q = reinterpret_cast<float4 *>(p);
+    q[0] = make_float4(v[0].hi, v[0].lo, v[1].hi, v[1].lo);
+    q[1] = make_float4(v[2].hi, v[2].lo, v[3].hi, v[3].lo);
+}
+struct __align__(16) df2 {
+    df x, y;
+};
 template <typename T> struct V2;
+template <> struct V2<df> {
+    using t = df2;
+};
 template <> struct V2<double> {
     using t = double2;
 };
@@ -378,7 +440,7 @@ __device__ __forceinline__ void lp_limit(const DMesh &M, int i, int ne, const T 
 }
 
 template <typename T, int MJ, bool LP, bool UNI>
-__global__ void __launch_bounds__(cell_threads<T>(), sizeof(T) == 4 ? EBB_CELL_MINB_F : EBB_CELL_MINB_D) k_cell(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, int limit)
+__global__ void __launch_bounds__(cell_threads<T>(), cell_minb<T>()) k_cell(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, int limit)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool act = i < M.C;
@@ -772,7 +834,7 @@ __device__ void boundary_flux(const DMesh &M, const DPhys &P, const DArrays &A, 
 }
 
 template <typename T>
-__global__ void __launch_bounds__(flux_threads<T>(), sizeof(T) == 4 ? EBB_FLUX_MINB_F : EBB_FLUX_MINB_D) k_flux(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, int nbi)
+__global__ void __launch_bounds__(flux_threads<T>(), flux_minb<T>()) k_flux(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, int nbi)
 {
     if ((int)blockIdx.x >= nbi) {
         grid_dep_release();
@@ -866,7 +928,7 @@ __device__ __forceinline__ float warp_maxf(float v)
 // integrators.d.  Split path: qin is the FP32 stage input, q64 is updated in FP64 and
 // the next stage input (qout) is its FP32 rounding.
 template <typename T, int ST, int MJ, bool UNI>
-__global__ void __launch_bounds__(UPD_THREADS, sizeof(T) == 4 ? EBB_UPD_MINB_F : EBB_UPD_MINB_D) k_update(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, T *qout,
+__global__ void __launch_bounds__(UPD_THREADS, upd_minb<T>()) k_update(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, T *qout,
                                                        int dt_update, int need_dt, int final_stage)
 {
     constexpr bool SPLIT = sizeof(T) == 4;
@@ -1103,7 +1165,7 @@ __global__ void __launch_bounds__(UPD_THREADS, sizeof(T) == 4 ? EBB_UPD_MINB_F :
                     for (int k = 0; k < 4; k++) out[k] = q0[k] + hh * ((double)k1[k] + Rd[k]);
                 } else {
 #pragma unroll
-                    for (int k = 0; k < 4; k++) out[k] = q0[k] + hh * (k1[k] + R[k]);
+                    for (int k = 0; k < 4; k++) out[k] = q0[k] + hh * (double)(k1[k] + R[k]);
                 }
             } else if (ST == ST_TVD_1) {
                 if (SPLIT) st4(aux + 4 * (size_t)i, R);
@@ -1117,7 +1179,10 @@ __global__ void __launch_bounds__(UPD_THREADS, sizeof(T) == 4 ? EBB_UPD_MINB_F :
 #pragma unroll
                     for (int k = 0; k < 4; k++) qfe[k] = q0[k] + h * (double)r1[k];
                 } else {
-                    ld4(reinterpret_cast<const double *>(qin) + 4 * (size_t)i, qfe);
+                    T qf[4];
+                    ld4(qin + 4 * (size_t)i, qf);
+#pragma unroll
+                    for (int k = 0; k < 4; k++) qfe[k] = (double)qf[k];
                 }
 #pragma unroll
                 for (int k = 0; k < 4; k++) out[k] = 0.5 * (q0[k] + qfe[k] + h * Rd[k]);
@@ -1147,12 +1212,12 @@ __global__ void __launch_bounds__(UPD_THREADS, sizeof(T) == 4 ? EBB_UPD_MINB_F :
                     for (int k = 0; k < 4; k++) out[k] = q0[k] + hh * ((double)acc[k] + Rd[k]);
                 } else {
 #pragma unroll
-                    for (int k = 0; k < 4; k++) out[k] = q0[k] + hh * (acc[k] + R[k]);
+                    for (int k = 0; k < 4; k++) out[k] = q0[k] + hh * (double)(acc[k] + R[k]);
                 }
             }
             if (final_stage) {
                 st4(A.q64 + 4 * (size_t)i, out);
-                if (SPLIT) {
+                if (!is_fp64<T>) {  // the double-float shadow of the solution
                     T o[4] = {(T)out[0], (T)out[1], (T)out[2], (T)out[3]};
                     st4(qout + 4 * (size_t)i, o);
                 }

@@ -16,6 +16,8 @@
 #pragma once
 #include <stdint.h>
 
+#include "dfloat.h"
+
 #define EBB_NOERR 0xFFFFFFFFFFFFFFFFull
 #define EBB_REC_CAP 4096
 #define EBB_RED_THREADS 256
@@ -64,6 +66,7 @@ struct DPhys {
                         // thread spends FP64-pipe time converting the doubles
     double gP, c43gP, m1gP, p43mgP, omgP;  // 1.4/pr, -4/3 + gP, -1 + gP, 4/3 - gP, 1 - gP (FP64
                                            // viscous flux constants, rounded once on the host)
+    ebbdf::df gPw, c43gPw, m1gPw, p43mgPw, omgPw, muw;  // the same as double-floats (df path)
 };
 
 // device-resident scalar state of the time loop
@@ -143,7 +146,13 @@ int launch_update<double>(const DMesh &, const DPhys &, const DArrays &, int, co
 template <>
 int launch_update<float>(const DMesh &, const DPhys &, const DArrays &, int, const float *, float *, int, int, int,
                          void *);
-int launch_step_end(const DMesh &M, const DArrays &A, int nred_blocks, int split, void *stream);
+template <> int launch_cell<ebbdf::df>(const DMesh &, const DPhys &, const DArrays &, const ebbdf::df *, int, void *);
+template <> int launch_flux<ebbdf::df>(const DMesh &, const DPhys &, const DArrays &, const ebbdf::df *, void *);
+template <>
+int launch_update<ebbdf::df>(const DMesh &, const DPhys &, const DArrays &, int, const ebbdf::df *, ebbdf::df *, int,
+                             int, int, void *);
+// precision: EBB_PREC_FP64, EBB_PREC_SPLIT or EBB_PREC_DF (the type of the stored edge fluxes)
+int launch_step_end(const DMesh &M, const DArrays &A, int nred_blocks, int precision, void *stream);
 // ebb-reconstruct: edge values (reference edge order) and node values
 template <typename T>
 int launch_recon(const DMesh &M, const DArrays &A, const T *qs, double *edge_out, int n_nodes, const int32_t *off,
@@ -157,6 +166,10 @@ template <>
 int launch_recon<float>(const DMesh &, const DArrays &, const float *, double *, int, const int32_t *,
                         const int32_t *, const uint8_t *, const double *, const double *, double *,
                         unsigned long long *, void *);
+template <>
+int launch_recon<ebbdf::df>(const DMesh &, const DArrays &, const ebbdf::df *, double *, int, const int32_t *,
+                            const int32_t *, const uint8_t *, const double *, const double *, double *,
+                            unsigned long long *, void *);
 int update_grid(const DMesh &M);
 int launch_flux_batch(int kind, int64_t n, const double *qL, const double *qR, const double *nrm, double *F,
                       double *s, void *stream);
@@ -165,6 +178,9 @@ int update_blocks(int C);
 int launch_permute4(const double *src, double *dst, const int32_t *idx, int64_t n, int gather, void *stream);
 int launch_to_float4(const double *src, float *dst, int64_t n, void *stream);
 int launch_to_double4(const float *src, double *dst, int64_t n, void *stream);
+// q64 (device order) -> its double-float shadow (dst: 4 double-floats per cell)
+int launch_to_df4(const double *src, void *dst, int64_t n, void *stream);
+int launch_from_df4(const void *src, double *dst, int64_t n, void *stream);
 // state in reference order (src, possibly page-locked host memory) -> device order
 // q64[iperm[j]] = src[j], plus its FP32 copy when qs1 is given; and back
 int launch_load_state(const double *src, double *q64, float *qs1, const int32_t *iperm, int64_t n, void *stream);

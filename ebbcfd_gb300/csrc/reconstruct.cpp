@@ -158,8 +158,8 @@ int ebb_reconstruct(ebb_solver *s, const ebb_mesh *mesh, const char *mmsh_path, 
     if (!q_out && !mmsh_path && !esln_path) return EBB_OK;  // size query
 
     // device buffers of the reconstruction (post-processing: allocated per call)
-    const bool split = s->precision == EBB_PREC_SPLIT;
-    const size_t rs = split ? sizeof(float) : sizeof(double);
+    const bool split = s->precision == EBB_PREC_SPLIT, dfp = s->precision == EBB_PREC_DF;
+    const size_t rs = split ? sizeof(float) : sizeof(double);  // a double-float is 8 bytes
     std::vector<double> cxy(2 * C);
     for (int64_t i = 0; i < C; i++) {  // centroids in device cell order
         cxy[2 * i] = topo.cx[s->perm[i]];
@@ -189,6 +189,8 @@ int ebb_reconstruct(ebb_solver *s, const ebb_mesh *mesh, const char *mmsh_path, 
     // stepMesh: one evaluation on the resident state with gradients and limiters kept
     if (split)
         launch_to_float4(s->A.q64, reinterpret_cast<float *>(s->A.qs), C, st);
+    else if (dfp)
+        launch_to_df4(s->A.q64, s->A.qs, C, st);
     else
         cudaMemcpyAsync(s->A.qs, s->A.q64, 4 * C * sizeof(double), cudaMemcpyDeviceToDevice, st);
     const int32_t need_grad = s->P.need_grad;
@@ -201,6 +203,10 @@ int ebb_reconstruct(ebb_solver *s, const ebb_mesh *mesh, const char *mmsh_path, 
                                         (const int32_t *)P_(3), (const int32_t *)P_(4), (const uint8_t *)P_(5),
                                         (const double *)P_(6), (const double *)P_(7), (double *)P_(2),
                                         (unsigned long long *)P_(8), st)
+            : dfp ? launch_recon<ebbdf::df>(s->M, s->A, reinterpret_cast<const ebbdf::df *>(s->A.qs), (double *)P_(1),
+                                            (int)nU, (const int32_t *)P_(3), (const int32_t *)P_(4),
+                                            (const uint8_t *)P_(5), (const double *)P_(6), (const double *)P_(7),
+                                            (double *)P_(2), (unsigned long long *)P_(8), st)
                   : launch_recon<double>(s->M, s->A, reinterpret_cast<const double *>(s->A.qs), (double *)P_(1),
                                          (int)nU, (const int32_t *)P_(3), (const int32_t *)P_(4),
                                          (const uint8_t *)P_(5), (const double *)P_(6), (const double *)P_(7),

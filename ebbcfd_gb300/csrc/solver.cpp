@@ -90,6 +90,7 @@ int state_in(ebb_solver *s, const double *q, int64_t c0, int64_t n)
     }
     float *qs1 = s->precision == EBB_PREC_SPLIT ? reinterpret_cast<float *>(s->A.qs1) : nullptr;
     CKL(launch_load_state(src, s->A.q64, qs1, s->d_iperm + c0, n, s->stream));
+    if (s->precision == EBB_PREC_DF) CKL(launch_to_df4(s->A.q64, s->A.qs1, s->C, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     return EBB_OK;
 }
@@ -160,14 +161,16 @@ template <typename T> int integrator_stages_t(ebb_solver *s)
 
 int integrator_stages(ebb_solver *s)
 {
-    return s->precision == EBB_PREC_SPLIT ? integrator_stages_t<float>(s) : integrator_stages_t<double>(s);
+    if (s->precision == EBB_PREC_SPLIT) return integrator_stages_t<float>(s);
+    if (s->precision == EBB_PREC_DF) return integrator_stages_t<ebbdf::df>(s);
+    return integrator_stages_t<double>(s);
 }
 
 int one_loop_step(ebb_solver *s)
 {
     int r = integrator_stages(s);
     if (r) return r;
-    CKL(launch_step_end(s->M, s->A, s->nred, s->precision == EBB_PREC_SPLIT, s->stream));
+    CKL(launch_step_end(s->M, s->A, s->nred, s->precision, s->stream));
     return EBB_OK;
 }
 
@@ -177,6 +180,10 @@ int residual_kernels(ebb_solver *s, int limit, int dt_update)
     if (s->precision == EBB_PREC_SPLIT) {
         float *qs = reinterpret_cast<float *>(s->A.qs);
         return run_stage_t<float>(s, ST_RESID, qs, nullptr, limit, dt_update, 1, 0);
+    }
+    if (s->precision == EBB_PREC_DF) {
+        ebbdf::df *qs = reinterpret_cast<ebbdf::df *>(s->A.qs);
+        return run_stage_t<ebbdf::df>(s, ST_RESID, qs, nullptr, limit, dt_update, 1, 0);
     }
     double *qs = reinterpret_cast<double *>(s->A.qs);
     return run_stage_t<double>(s, ST_RESID, qs, nullptr, limit, dt_update, 1, 0);
@@ -287,7 +294,7 @@ template <typename T> int profile_t(ebb_solver *s, int32_t n_rep, double *ms)
             if (k == 0) CKL(launch_cell<T>(s->M, s->P, s->A, qs, 1, s->stream));
             if (k == 1) CKL(launch_flux<T>(s->M, s->P, s->A, qs, s->stream));
             if (k == 2) CKL(launch_update<T>(s->M, s->P, s->A, ST_RK2_1, qs, scratch, 1, 1, 0, s->stream));
-            if (k == 3) CKL(launch_step_end(s->M, s->A, s->nred, sizeof(T) == 4, s->stream));
+            if (k == 3) CKL(launch_step_end(s->M, s->A, s->nred, s->precision, s->stream));
         }
         CK(cudaEventRecord(ev[1], s->stream));
         CK(cudaEventSynchronize(ev[1]));
@@ -361,7 +368,7 @@ int ebb_batch_create(int32_t n, const ebb_mesh *const *meshes, const ebb_config 
     if (n <= 0 || !meshes || !cfgs) return EBB_ERR_ARG;
     for (int32_t k = 0; k < n; k++)
         if (!meshes[k]) return EBB_ERR_ARG;
-    if (precision != EBB_PREC_FP64 && precision != EBB_PREC_SPLIT) {
+    if (precision != EBB_PREC_FP64 && precision != EBB_PREC_SPLIT && precision != EBB_PREC_DF) {
         set_err(err, err_len, "unknown precision form");
         return EBB_ERR_ARG;
     }
@@ -481,10 +488,13 @@ int ebb_residual_device(ebb_solver *s, const double *q_dev, double *R_dev, doubl
 {
     if (!s || !q_dev || !R_dev) return EBB_ERR_ARG;
     if (s->n_inst != 1) return fail(s, EBB_ERR_ARG, "not available on a batch of several instances");
-    const bool split = s->precision == EBB_PREC_SPLIT;
+    const bool split = s->precision == EBB_PREC_SPLIT, dfp = s->precision == EBB_PREC_DF;
     if (split) {
         CKL(launch_permute4(q_dev, s->d_tmp, s->d_perm, s->C, 1, s->stream));
         CKL(launch_to_float4(s->d_tmp, reinterpret_cast<float *>(s->A.qs), s->C, s->stream));
+    } else if (dfp) {
+        CKL(launch_permute4(q_dev, s->d_tmp, s->d_perm, s->C, 1, s->stream));
+        CKL(launch_to_df4(s->d_tmp, s->A.qs, s->C, s->stream));
     } else {
         CKL(launch_permute4(q_dev, reinterpret_cast<double *>(s->A.qs), s->d_perm, s->C, 1, s->stream));
     }
@@ -492,6 +502,9 @@ int ebb_residual_device(ebb_solver *s, const double *q_dev, double *R_dev, doubl
     if (r) return r;
     if (split) {
         CKL(launch_to_double4(reinterpret_cast<const float *>(s->A.R), s->d_tmp, s->C, s->stream));
+        CKL(launch_permute4(s->d_tmp, R_dev, s->d_perm, s->C, 0, s->stream));
+    } else if (dfp) {
+        CKL(launch_from_df4(s->A.R, s->d_tmp, s->C, s->stream));
         CKL(launch_permute4(s->d_tmp, R_dev, s->d_perm, s->C, 0, s->stream));
     } else {
         CKL(launch_permute4(reinterpret_cast<const double *>(s->A.R), R_dev, s->d_perm, s->C, 0, s->stream));
@@ -617,7 +630,9 @@ int ebb_profile_kernels(ebb_solver *s, int32_t n_rep, double *ms)
         x.rec_enabled = 0;
     }
     if ((r = solver_write_all(s, h))) return r;
-    r = s->precision == EBB_PREC_SPLIT ? profile_t<float>(s, n_rep, ms) : profile_t<double>(s, n_rep, ms);
+    r = s->precision == EBB_PREC_SPLIT ? profile_t<float>(s, n_rep, ms)
+        : s->precision == EBB_PREC_DF  ? profile_t<ebbdf::df>(s, n_rep, ms)
+                                       : profile_t<double>(s, n_rep, ms);
     int r2 = solver_write_all(s, h0);
     return r ? r : r2;
 }
@@ -632,6 +647,11 @@ int ebb_get_face_states(ebb_solver *s, double *out)
         CK(cudaMemcpyAsync(g.data(), s->A.face, n * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
         CK(cudaStreamSynchronize(s->stream));
         for (size_t k = 0; k < n; k++) f[k] = g[k];
+    } else if (s->precision == EBB_PREC_DF) {
+        std::vector<ebbdf::df> g(n);
+        CK(cudaMemcpyAsync(g.data(), s->A.face, n * sizeof(ebbdf::df), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        for (size_t k = 0; k < n; k++) f[k] = (double)g[k];
     } else {
         CK(cudaMemcpyAsync(f.data(), s->A.face, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
         CK(cudaStreamSynchronize(s->stream));
@@ -651,6 +671,11 @@ int ebb_get_edge_fluxes(ebb_solver *s, double *out)
         CK(cudaMemcpyAsync(g.data(), s->A.fl, n * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
         CK(cudaStreamSynchronize(s->stream));
         for (size_t k = 0; k < n; k++) f[k] = g[k];
+    } else if (s->precision == EBB_PREC_DF) {
+        std::vector<ebbdf::df> g(n);
+        CK(cudaMemcpyAsync(g.data(), s->A.fl, n * sizeof(ebbdf::df), cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        for (size_t k = 0; k < n; k++) f[k] = (double)g[k];
     } else {
         CK(cudaMemcpyAsync(f.data(), s->A.fl, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
         CK(cudaStreamSynchronize(s->stream));

@@ -55,7 +55,7 @@ enum : int
 
 enum : int { EBB_FLUX_RUSANOV = 0, EBB_FLUX_ROE = 1 }                                  // fluxList
 enum : int { EBB_INT_EULER = 0, EBB_INT_RK2 = 1, EBB_INT_RK2_TVD = 2, EBB_INT_RK4 = 3 } // integratorList
-enum : int { EBB_PREC_FP64 = 0, EBB_PREC_SPLIT = 1 }
+enum : int { EBB_PREC_FP64 = 0, EBB_PREC_SPLIT = 1, EBB_PREC_DF = 2 }
 enum : int { EBB_MMS_NONE = 0, EBB_MMS_REFERENCE = 1, EBB_MMS_SINE = 2 }
 
 struct ebb_boundary

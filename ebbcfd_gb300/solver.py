@@ -19,7 +19,7 @@ import numpy as np
 
 from . import _lib
 
-PRECISION = {"fp64": 0, "split": 1}
+PRECISION = {"fp64": 0, "split": 1, "df": 2}
 FLUX = {"rusanovFlux": 0, "roeFlux": 1}
 INTEGRATOR = {"Euler": 0, "RK2": 1, "RK2_TVD": 2, "RK4": 3}
 BC = {"fullState": 0, "constP": 1, "inviscidWall": 2, "viscidWall": 3, "symmetry": 4, "tpInflow": 5, "dirichlet": 6}

@@ -71,8 +71,10 @@ typedef enum { EBB_INT_EULER = 0, EBB_INT_RK2 = 1, EBB_INT_RK2_TVD = 2, EBB_INT_
 
 /* precision forms */
 typedef enum {
-    EBB_PREC_FP64 = 0, /* plain FP64 path, same operation order as the reference */
-    EBB_PREC_SPLIT = 1 /* FP32 flux/gradient/limiter arithmetic, FP64 geometry, state update and reductions */
+    EBB_PREC_FP64 = 0,  /* plain FP64 path, same operation order as the reference */
+    EBB_PREC_SPLIT = 1, /* FP32 flux/gradient/limiter arithmetic, FP64 geometry, state update and reductions */
+    EBB_PREC_DF = 2     /* flux/gradient/limiter arithmetic on double-floats (pairs of FP32 numbers, ~46
+                           significant bits) on the FP32 pipe; FP64 geometry, state update and reductions */
 } ebb_precision;
 
 /* manufactured-solution fields used by Dirichlet boundaries and the source term */
