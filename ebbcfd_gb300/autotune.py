@@ -5,17 +5,18 @@ blocks per SM requested through __launch_bounds__.  The split kernels are bound 
 memory latency, so the warps an SM keeps in flight decide their speed; the block
 size and the minimum-blocks argument (a cap on registers per thread -- too low a cap
 spills) set that at compile time.  The FP64 kernels are bound by the FP64 pipe; a few
-more warps can still fill its gaps.  k_update's block size (256 or 512) is also the
+more warps can still fill its gaps.  The double-float kernels run long dependent FP32
+sequences with many live values: few warps, and a cap that does not spill.  k_update's block size (256 or 512) is also the
 size of the per-block reduction trees and of the batched arena's update-block map, so
-one value serves both precision forms in a build.
+one value serves all precision forms in a build.
 
 Every row of candidate settings is one variant of the library (under
 ebbcfd_gb300/_build/tune_<k>/, with -DEBB_* overrides; the variants compile in
-parallel).  Each variant's kernels of both precision forms are timed with
+parallel).  Each variant's kernels of the three precision forms are timed with
 ebb_profile_kernels (CUDA events on the solver stream, best of three rounds) on the
 headline workload -- the 4.0M-cell Navier-Stokes plate (--workload wedge: the 1.0M
 Mach 2.5 wedge) -- and per kernel the fastest setting over the rows is kept.  The
-kernels are independent launches, so one variant measures all six at once.  Register
+kernels are independent launches, so one variant measures all nine at once.  Register
 allocation and block size change no FP64 result bit (the kernels stay bitwise equal to
 the oracle); the update block size changes the order of the RMS residual sums only.
 
@@ -35,7 +36,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 # per precision form and kernel: candidate (threads per block, minimum blocks per SM),
 # one entry per row (threads x blocks <= 2048); the update kernel's threads come from
-# UPD_TB, shared by both forms
+# UPD_TB, shared by all forms
 CANDIDATES = {
     "split": {"cell": [(128, 8), (128, 10), (128, 6), (256, 4), (256, 3), (64, 16), (64, 12)],
               "flux": [(128, 12), (128, 10), (128, 8), (256, 6), (256, 4), (64, 20), (64, 16)],
@@ -43,12 +44,17 @@ CANDIDATES = {
     "fp64": {"cell": [(128, 5), (128, 1), (128, 6), (256, 2), (256, 3), (64, 8), (64, 10)],
              "flux": [(128, 1), (128, 4), (128, 5), (256, 2), (256, 1), (64, 8), (64, 6)],
              "update": [3, 1, 2, 2, 1, 4, 1]},
+    "df": {"cell": [(128, 2), (128, 1), (128, 3), (256, 1), (256, 2), (64, 4), (64, 6)],
+           "flux": [(128, 2), (128, 1), (128, 3), (256, 1), (256, 2), (64, 4), (64, 6)],
+           "update": [3, 1, 2, 2, 1, 4, 1]},
 }
 UPD_TB = [256, 256, 256, 512, 512, 256, 512]
 N_ROWS = len(UPD_TB)
 MACRO = {("split", "cell"): ("EBB_CELL_TB_F", "EBB_CELL_MINB_F"), ("split", "flux"): ("EBB_FLUX_TB_F", "EBB_FLUX_MINB_F"),
          ("fp64", "cell"): ("EBB_CELL_TB_D", "EBB_CELL_MINB_D"), ("fp64", "flux"): ("EBB_FLUX_TB_D", "EBB_FLUX_MINB_D"),
-         ("split", "update"): ("EBB_UPD_TB", "EBB_UPD_MINB_F"), ("fp64", "update"): ("EBB_UPD_TB", "EBB_UPD_MINB_D")}
+         ("df", "cell"): ("EBB_CELL_TB_W", "EBB_CELL_MINB_W"), ("df", "flux"): ("EBB_FLUX_TB_W", "EBB_FLUX_MINB_W"),
+         ("split", "update"): ("EBB_UPD_TB", "EBB_UPD_MINB_F"), ("fp64", "update"): ("EBB_UPD_TB", "EBB_UPD_MINB_D"),
+         ("df", "update"): ("EBB_UPD_TB", "EBB_UPD_MINB_W")}
 
 
 def setting(row):
@@ -104,7 +110,7 @@ def _measure(row, workload, cells):
         ms = (C.c_double * 4)()
         best = None
         for _ in range(3):
-            if L.ebb_profile_kernels(s.h, 20 if p == "split" else 3, ms):
+            if L.ebb_profile_kernels(s.h, {"split": 20, "df": 6, "fp64": 3}[p], ms):
                 raise RuntimeError("profiling failed")
             best = list(ms) if best is None else [min(a, b) for a, b in zip(best, ms)]
         s.close()
@@ -136,7 +142,7 @@ def tune(workload="plate", cells=None, out=None):
             choice[(prec, k)] = min(times, key=times.get)
             lines.append("// %s k_%s: " % (prec, k) +
                          ", ".join("%dx%d %.1f us" % (tb, b, t) for (tb, b), t in sorted(times.items())))
-    # one update block size for both forms: the one whose best total is smaller
+    # one update block size for all forms: the one whose best total is smaller
     upd = {}
     for tb in sorted(set(UPD_TB)):
         upd[tb] = sum(min(r["us"][p]["update"] for r in rows if r["setting"][p]["update"][0] == tb)
@@ -148,7 +154,7 @@ def tune(workload="plate", cells=None, out=None):
         choice[(p, "update")] = best[1]
     cells_txt = "%d-cell" % cells if cells else "default-size"
     text = ["// Generated by ebbcfd_gb300/autotune.py on the %s %s workload: device time per" % (cells_txt, workload),
-            "// launch of each kernel of both precision forms for each (threads per block) x (minimum",
+            "// launch of each kernel of the three precision forms for each (threads per block) x (minimum",
             "// resident blocks per SM requested through __launch_bounds__; 1 = the compiler's",
             "// register choice), best of three rounds of CUDA-event timing; fastest kept."] + lines
     text += ["// update block size %d (summed best update times: %s)" %
