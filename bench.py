@@ -789,12 +789,13 @@ def run_serve(args):
     """Served request stream: Poisson arrivals (seed 7, mean 40 req/s); 70% Euler bump
     channels, 30% Navier-Stokes cylinders (Re ~ U[50,200], Mach 0.2); cell counts
     log-uniform in [1e3, 2e6]; each stops at a 1e-8 residual drop or its step cap;
-    split precision, continued in plain FP64 once its residual levels off (the server's
-    FP64 finishing); admission capped at 150 GB.  Latency = result in hand minus
-    scheduled arrival; service time = finish minus first admission.  The sequential
-    baselines solve the requests one at a time: each request's device time per step
-    alone (timed on a sample of steps) times the steps it ran -- all in plain FP64, or
-    in the served form (its split steps in split precision, the rest in FP64)."""
+    split precision, continued in plain FP64 (--finish df: double-float) once its
+    residual levels off (the server's finishing); admission capped at 150 GB.  Latency =
+    result in hand minus scheduled arrival; service time = finish minus first admission.
+    The sequential baselines solve the requests one at a time: each request's device
+    time per step alone (timed on a sample of steps) times the steps it ran -- all in
+    plain FP64, or in the served form (its split steps in split precision, the rest in
+    the finishing form)."""
     import ebbcfd_gb300 as E
     from ebbcfd_gb300 import _lib
     R = args.requests
@@ -819,7 +820,8 @@ def run_serve(args):
                           else cylinder_json(float(r), integrator=args.serve_integrator))
             for k, m, r in zip(kinds, machs, res)]
     L = _lib.load()
-    sv = E.EbbServer("split", hbm_budget=int(150e9), build_threads=8, finish_fp64=int(not args.no_finish))
+    sv = E.EbbServer("split", hbm_budget=int(150e9), build_threads=8, finish_fp64=int(not args.no_finish),
+                     finish_precision=args.finish)
     clocks = Clocks(0)
     clocks.start()
     tb = time.perf_counter()
@@ -851,11 +853,12 @@ def run_serve(args):
     it32 = np.array([min(done[k]["split_iterations"], done[k]["iterations"]) for k in range(R)])
     cu = float(sum(iters[k] * meshes[k].n_cells for k in range(R)))
     # sequential solves: per-step device time alone x steps run (plain FP64 throughout,
-    # or split steps in split precision and the finishing steps in FP64)
+    # or split steps in split precision and the finishing steps in the finishing form)
     per = seq_ms_per_step(L, E, meshes, cfgs, "fp64", args.seq_steps, 3)
     per32 = seq_ms_per_step(L, E, meshes, cfgs, "split", args.seq_steps, 3)
+    perF = per if args.finish == "fp64" else seq_ms_per_step(L, E, meshes, cfgs, args.finish, args.seq_steps, 3)
     seq_s = float(sum(per[k] * iters[k] for k in range(R)) / 1e3)
-    seq32_s = float(sum(per32[k] * it32[k] + per[k] * (iters[k] - it32[k]) for k in range(R)) / 1e3)
+    seq32_s = float(sum(per32[k] * it32[k] + perF[k] * (iters[k] - it32[k]) for k in range(R)) / 1e3)
     # error of the served (split) results against plain FP64 solves with the same stop
     # conditions, on the smallest requests (three bump channels, one cylinder: their
     # FP64 re-solves take seconds)
@@ -885,7 +888,8 @@ def run_serve(args):
             "cell_updates_per_s": cu / wall, "latency_p50_s": float(np.percentile(lat, 50)),
             "latency_p99_s": float(np.percentile(lat, 99)), "latency_max_s": float(lat.max()),
             "service_p50_s": float(np.percentile(svc, 50)), "service_p99_s": float(np.percentile(svc, 99)),
-            "finished_in_fp64": int(sum(done[k]["escalated"] == 2 for k in range(R))),
+            "finish_precision": args.finish,
+            "finished_after_stall": int(sum(done[k]["escalated"] == 2 for k in range(R))),
             "split_iteration_share": float(sum(it32[k] * meshes[k].n_cells for k in range(R)) / cu),
             "statuses": sorted(set(int(done[k]["status"]) for k in range(R))),
             "failed": [{"k": k, "kind": str(kinds[k]), "cells": meshes[k].n_cells, "status": int(done[k]["status"]),
@@ -951,6 +955,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-split", action="store_true")
+    ap.add_argument("--finish", default="fp64", choices=["fp64", "df"],
+                    help="serve: form a stalled split solve finishes in")
     ap.add_argument("--no-wedge", action="store_true")
     ap.add_argument("--no-df", action="store_true", help="skip the double-float precision form's leg")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
@@ -965,7 +971,7 @@ def main():
     ap.add_argument("--serve-integrator", default="RK2", choices=["Euler", "RK2", "RK2_TVD", "RK4"])
     ap.add_argument("--serve-flux", default="rusanovFlux", choices=["roeFlux", "rusanovFlux"])
     ap.add_argument("--batch-precision", default="split", choices=["split", "fp64"])
-    ap.add_argument("--no-finish", action="store_true", help="served split solves without FP64 finishing")
+    ap.add_argument("--no-finish", action="store_true", help="served split solves without finishing")
     args = ap.parse_args()
     args.steps_given = "--steps" in sys.argv
     args.cells_given = args.cells is not None

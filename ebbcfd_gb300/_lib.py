@@ -80,7 +80,7 @@ class ServerOptions(C.Structure):
     _fields_ = [("precision", C.c_int32), ("max_arenas", C.c_int32), ("max_batch", C.c_int32),
                 ("build_threads", C.c_int32), ("tick_ms", C.c_double), ("size_ratio", C.c_double),
                 ("arena_cells", C.c_int64), ("hbm_budget", C.c_uint64), ("escalate", C.c_int32),
-                ("finish_fp64", C.c_int32), ("stall_steps", C.c_int32)]
+                ("finish_fp64", C.c_int32), ("stall_steps", C.c_int32), ("finish_precision", C.c_int32)]
 
 
 class RequestResult(C.Structure):

@@ -265,7 +265,8 @@ int harvest(ebb_server *sv, ArenaRun &a)
                              !(rq.max_steps > 0 && st[k].iterations >= rq.max_steps) &&
                              !(rq.resid_drop > 0 && st[k].resid[0] <= rq.resid_drop * st[k].resid_first);
         if (stalled && sv->opt.finish_fp64 && rq.precision == EBB_PREC_SPLIT && rq.mesh) {
-            // continue in plain FP64 from the current state (same id)
+            // continue in the finishing form (plain FP64 or double-float) from the
+            // current state (same id)
             auto next = std::make_shared<Request>();
             next->id = rq.id;
             next->mesh = std::move(rq.mesh);
@@ -274,7 +275,7 @@ int harvest(ebb_server *sv, ArenaRun &a)
             next->resid_drop = rq.resid_drop;
             next->submit_s = rq.submit_s;
             next->admit_s = rq.admit_s;
-            next->precision = EBB_PREC_FP64;
+            next->precision = sv->opt.finish_precision;
             next->escalated = 2;
             next->split_iterations = st[k].iterations;
             next->resume = st[k];
@@ -409,6 +410,7 @@ void ebb_server_options_defaults(ebb_server_options *o)
     o->hbm_budget = 150000000000ull;
     o->finish_fp64 = 1;
     o->stall_steps = 1000;
+    o->finish_precision = EBB_PREC_FP64;
 }
 
 int ebb_server_create(const ebb_server_options *o, ebb_server **out, char *err, size_t err_len)
@@ -426,7 +428,8 @@ int ebb_server_create(const ebb_server_options *o, ebb_server **out, char *err, 
     else
         ebb_server_options_defaults(&sv->opt);
     ebb_server_options &p = sv->opt;
-    if ((p.precision != EBB_PREC_FP64 && p.precision != EBB_PREC_SPLIT) || p.max_arenas <= 0 || p.max_batch <= 0 ||
+    if ((p.precision != EBB_PREC_FP64 && p.precision != EBB_PREC_SPLIT && p.precision != EBB_PREC_DF) ||
+        (p.finish_precision != EBB_PREC_FP64 && p.finish_precision != EBB_PREC_DF) || p.max_arenas <= 0 || p.max_batch <= 0 ||
         p.build_threads <= 0 || !(p.tick_ms > 0) || !(p.size_ratio >= 1) || p.arena_cells <= 0) {
         delete sv;
         set_err(err, err_len, "invalid server options");

@@ -150,6 +150,7 @@ struct ebb_server_options
     int escalate;
     int finish_fp64;
     int stall_steps;
+    int finish_precision;
 }
 
 struct ebb_request_result

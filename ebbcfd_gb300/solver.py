@@ -418,7 +418,7 @@ class EbbServer:
         L.ebb_server_options_defaults(C.byref(o))
         o.precision = PRECISION[precision]
         for k, v in options.items():
-            setattr(o, k, v)
+            setattr(o, k, PRECISION[v] if k == "finish_precision" and isinstance(v, str) else v)
         h = C.c_void_p()
         err = C.create_string_buffer(512)
         _check(L.ebb_server_create(C.byref(o), C.byref(h), err, 512), err.value.decode())

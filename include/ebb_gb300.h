@@ -301,7 +301,7 @@ int ebb_batch_footprint(int32_t n, const ebb_mesh *const *meshes, const ebb_conf
 typedef struct ebb_server ebb_server;
 
 typedef struct ebb_server_options {
-    int32_t precision;     /* EBB_PREC_FP64 or EBB_PREC_SPLIT (default split) */
+    int32_t precision;     /* EBB_PREC_FP64, EBB_PREC_SPLIT or EBB_PREC_DF (default split) */
     int32_t max_arenas;    /* arenas on the device at once (default 32) */
     int32_t max_batch;     /* instances per arena at most (default 512) */
     int32_t build_threads; /* host threads laying out submitted meshes (default 4) */
@@ -315,10 +315,13 @@ typedef struct ebb_server_options {
                               residual, after falling at least 1000-fold from its first
                               iteration, makes no new minimum for stall_steps iterations (it
                               has levelled off at the FP32 rounding of its increments) continues in
-                              plain FP64 from its current state -- same id, iteration count,
-                              time and first-iteration residual -- until the drop, its step
-                              limit or tEnd (default 1) */
+                              finish_precision from its current state -- same id, iteration
+                              count, time and first-iteration residual -- until the drop, its
+                              step limit or tEnd (default 1) */
     int32_t stall_steps;   /* default 1000 */
+    int32_t finish_precision; /* form of that continuation: EBB_PREC_FP64 (default) or
+                                 EBB_PREC_DF (double-float: about 2.8x FP64's speed, within
+                                 ~1e-11 of its forces) */
 } ebb_server_options;
 
 typedef struct ebb_request_result {
@@ -332,7 +335,8 @@ typedef struct ebb_request_result {
     double submit_s, admit_s, finish_s; /* server clock: seconds since ebb_server_create */
     int32_t precision;                  /* precision form of the solve that produced the result */
     int32_t escalated;                  /* 1: re-solved in FP64 after a split-precision error;
-                                           2: finished in FP64 after its split solve stalled */
+                                           2: finished in the finishing form (precision) after
+                                              its split solve stalled */
     int64_t split_iterations;           /* iterations run in split precision */
     char msg[96];
 } ebb_request_result;

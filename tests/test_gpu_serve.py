@@ -165,9 +165,9 @@ def test_split_error_escalates_to_fp64():
         sv.close()
 
 
-def _serve_all(reqs, **opts):
+def _serve_all(reqs, precision="split", **opts):
     """Submit every (mesh, cfg, max_steps, resid_drop) at once; run to completion."""
-    sv = E.EbbServer("split", **opts)
+    sv = E.EbbServer(precision, **opts)
     ids = {sv.submit(m, c, n, d): k for k, (m, c, n, d) in enumerate(reqs)}
     out = {}
     for _ in range(1000000):
@@ -203,3 +203,25 @@ def test_stalled_split_solve_finishes_in_fp64():
     for f in ("iterations", "split_iterations", "t", "drag", "lift", "done_reason", "escalated"):
         assert r2[f] == r[f], f
     assert mix[0][0]["done_reason"] == 2 and mix[2][0]["done_reason"] == 3
+
+
+def test_stalled_split_solve_finishes_in_df():
+    """The same stalled split solve with the double-float form as the finishing form:
+    the split phase is the same (same split iterations), the continuation retires at the
+    drop in double-float, and its converged forces agree with the FP64-finished solve's.
+    A solve served in double-float from the start reaches the drop without finishing."""
+    m = meshgen.bump_channel(1500, h=0.05, seed=11).to_solver_mesh()
+    c = bump_cfg(0.5, flux="rusanovFlux")
+    drop, cap = 1e-8, 200000
+    r64, q64 = _serve_all([(m, c, cap, drop)], tick_ms=2.0)[0]
+    rdf, qdf = _serve_all([(m, c, cap, drop)], tick_ms=2.0, finish_precision="df")[0]
+    assert rdf["status"] == 0 and rdf["done_reason"] == 3, rdf
+    assert rdf["escalated"] == 2 and rdf["precision"] == 2
+    assert rdf["split_iterations"] == r64["split_iterations"]
+    assert rdf["resid"][0] <= drop * rdf["resid_first"]
+    assert abs(rdf["drag"] - r64["drag"]) <= 1e-6 * abs(r64["drag"])
+    assert np.abs(qdf - q64).max() <= 1e-6 * np.abs(q64).max()
+    r, q = _serve_all([(m, c, cap, drop)], precision="df", tick_ms=2.0)[0]
+    assert r["status"] == 0 and r["done_reason"] == 3 and r["escalated"] == 0 and r["precision"] == 2, r
+    assert r["split_iterations"] == 0 and r["iterations"] < cap
+    assert abs(r["drag"] - r64["drag"]) <= 1e-6 * abs(r64["drag"])
