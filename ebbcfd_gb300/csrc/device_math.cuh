@@ -37,7 +37,9 @@ template <> struct K<df> {  // the double constants, as double-floats
 // Quotients by one divisor.  FP64: one correctly rounded reciprocal of the divisor
 // serves every quotient (fdiv.h: Markstein's correction per quotient), which gives the
 // IEEE quotient bit for bit at about a third of the FP64 instructions of a division
-// per extra quotient; FP32: plain division, as the split path's flags compile it.
+// per extra quotient; FP32: plain division, as the split path's flags compile it;
+// double-float: one double-word reciprocal and a double-word product per quotient
+// (relative error a few units of 2^-46, a third of a double-word division's cost).
 template <typename T> struct Div {
     T b;
     __device__ __forceinline__ explicit Div(T d) : b(d) {}
@@ -48,12 +50,18 @@ template <> struct Div<double> {
     __device__ __forceinline__ explicit Div(double d) : R(ebbdiv::recip(d)) {}
     __device__ __forceinline__ double operator()(double a) const { return ebbdiv::div(a, R); }
 };
+template <> struct Div<df> {
+    df r;
+    __device__ __forceinline__ explicit Div(df d) : r(df(1.0f) / d) {}
+    __device__ __forceinline__ df operator()(df a) const { return a * r; }
+};
 
 // x / 2 = 0.5 x.  FP64: on the integer pipe -- for every x whose half is a normal
 // number the product is exact and is x with its exponent field lowered by one; zeros
 // are returned as they are (0.5 * +-0 = +-0).  Subnormal or tiny (biased exponent < 2),
 // infinite and NaN values take the FP64 multiply, behind a warp vote so that a warp
-// holding none issues no FP64 instruction.  FP32: the multiply.
+// holding none issues no FP64 instruction.  FP32: the multiply.  Double-float: both
+// words halved (exact but below FP32's normal range).
 template <typename T> __device__ __forceinline__ T half(T x) { return T(0.5) * x; }
 template <> __device__ __forceinline__ double half<double>(double x)
 {
@@ -67,6 +75,7 @@ template <> __device__ __forceinline__ double half<double>(double x)
     }
     return y;
 }
+template <> __device__ __forceinline__ df half<df>(df x) { return df(0.5f * x.hi, 0.5f * x.lo); }
 
 template <typename T> __device__ __forceinline__ T dsqrt(T x) { return sqrt(x); }
 template <> __device__ __forceinline__ float dsqrt<float>(float x) { return sqrtf(x); }

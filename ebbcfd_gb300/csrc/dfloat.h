@@ -1,6 +1,9 @@
 // dfloat.h -- double-float arithmetic: a value is the unevaluated sum hi + lo of two
-// FP32 numbers with |lo| <= ulp(hi) / 2, about 46 significant bits (measured: every
-// operation below within 2^-46 relative of the exact result, cancellation included).
+// FP32 numbers with |lo| <= ulp(hi) / 2, about 46 significant bits.  Error bounds
+// (checked on the host against exact rational arithmetic): a product, quotient or square
+// root within a few units of 2^-46 of the exact result, relative; a sum or difference
+// within a few units of 2^-46 of |a| + |b| -- the operands' own representation error,
+// so under cancellation the result is as accurate as its operands allow.
 //
 // GB300 executes FP32 at 64 times its FP64 rate, so an operation that costs 8-25 FP32
 // instructions still takes far less pipe time than one FP64 instruction.  The
@@ -65,14 +68,15 @@ EBB_DF_HD df two_prod(float a, float b)
     return df(p, fmaf(a, b, -p));
 }
 
+// Dekker's addition: the high words summed exactly, the low words added to the error
+// term, one renormalisation (11 FP32 operations).  Its error is bounded by the low
+// words' rounding, relative to |a| + |b|; the two-sum of the low words that would make
+// it relative to |a + b| costs 9 more operations and buys nothing here, since every
+// operand already carries a representation error of that size.
 EBB_DF_HD df operator+(df a, df b)
 {
-    df s = two_sum(a.hi, b.hi);
-    const df t = two_sum(a.lo, b.lo);
-    s.lo += t.hi;
-    s = fast_two_sum(s.hi, s.lo);
-    s.lo += t.lo;
-    return fast_two_sum(s.hi, s.lo);
+    const df s = two_sum(a.hi, b.hi);
+    return fast_two_sum(s.hi, s.lo + (a.lo + b.lo));
 }
 EBB_DF_HD df operator-(df a) { return df(-a.hi, -a.lo); }
 EBB_DF_HD df operator-(df a, df b) { return a + (-b); }
@@ -82,16 +86,24 @@ EBB_DF_HD df operator*(df a, df b)
     p.lo = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, p.lo));
     return fast_two_sum(p.hi, p.lo);
 }
+// a double-float times an FP32 number
+EBB_DF_HD df mul_f(df a, float b)
+{
+    df p = two_prod(a.hi, b);
+    p.lo = fmaf(a.lo, b, p.lo);
+    return fast_two_sum(p.hi, p.lo);
+}
 // a / b: a first quotient from the FP32 reciprocal, two double-word corrections
 EBB_DF_HD df operator/(df a, df b)
 {
     const float y = 1.0f / b.hi;
     const float q1 = a.hi * y;
-    const df r = a - b * df(q1);
+    const df r = a - mul_f(b, q1);
     const float q2 = r.hi * y;
-    const df r2 = r - b * df(q2);
+    const df r2 = r - mul_f(b, q2);
     const float q3 = r2.hi * y;
-    return fast_two_sum(q1, q2) + df(q3);
+    const df q = fast_two_sum(q1, q2);
+    return fast_two_sum(q.hi, q.lo + q3);
 }
 EBB_DF_HD df &operator+=(df &a, df b) { return a = a + b; }
 EBB_DF_HD df &operator-=(df &a, df b) { return a = a - b; }

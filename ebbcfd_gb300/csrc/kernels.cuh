@@ -183,6 +183,20 @@ __device__ __forceinline__ float d2f_int(double x)
     return __uint_as_float(ebbbits::d2f_bits((uint32_t)__double2hiint(x), (uint32_t)__double2loint(x)));
 }
 
+// The FP64 value of a stage-kernel value and back.  Double-float: the word conversions
+// on the integer pipe (exact), so each direction costs one FP64 add or subtract instead
+// of two or three FP64-pipe conversions and an add; below FP32's normal range the
+// words flush to zero, and an infinite or NaN value keeps a zero low word.
+template <typename T> __device__ __forceinline__ double to_f64(T x) { return (double)x; }
+template <> __device__ __forceinline__ double to_f64<df>(df x) { return f2d_int(x.hi) + f2d_int(x.lo); }
+template <typename T> __device__ __forceinline__ T from_f64(double x) { return (T)x; }
+template <> __device__ __forceinline__ df from_f64<df>(double x)
+{
+    const float h = d2f_int(x);
+    const float l = d2f_int(x - f2d_int(h));
+    return df(h, isfinite(h) ? l : 0.0f);
+}
+
 // 4-vector loads/stores: two 16-byte accesses for double, one for float
 __device__ __forceinline__ void ld4(const double *p, double v[4])
 {
@@ -1045,7 +1059,7 @@ __global__ void __launch_bounds__(UPD_THREADS, upd_minb<T>()) k_update(DMesh M, 
                 if (SPLIT)
                     fdtc = (float)c;
                 else
-                    dtc = (double)c;
+                    dtc = to_f64(c);
             }
             if (P.local_ts && dt_update) cdt[i] = isnan(c) ? T(0.0) : c;
         }
@@ -1053,6 +1067,12 @@ __global__ void __launch_bounds__(UPD_THREADS, upd_minb<T>()) k_update(DMesh M, 
 #pragma unroll
             for (int k = 0; k < 4; k++)
                 if ((float)fabs(r[k]) > frm) frm = (float)fabs(r[k]);
+        } else if constexpr (is_df<T>) {  // the largest |r| found in double-float, one conversion
+            T m = T(0.0f);
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                if (fabs(r[k]) > m) m = fabs(r[k]);
+            rm = to_f64(m);
         } else {
 #pragma unroll
             for (int k = 0; k < 4; k++)
@@ -1146,9 +1166,9 @@ __global__ void __launch_bounds__(UPD_THREADS, upd_minb<T>()) k_update(DMesh M, 
             double q0[4], Rd[4], out[4];
             ld4(A.q64 + 4 * (size_t)i, q0);
 #pragma unroll
-            for (int k = 0; k < 4; k++) Rd[k] = (double)R[k];
+            for (int k = 0; k < 4; k++) Rd[k] = to_f64(R[k]);
             const double dt = st->dt;
-            const double h = P.local_ts ? (double)cdt[i] : dt;
+            const double h = P.local_ts ? to_f64(cdt[i]) : dt;
             if (ST == ST_EULER) {
 #pragma unroll
                 for (int k = 0; k < 4; k++) out[k] = q0[k] + h * Rd[k];
@@ -1165,7 +1185,7 @@ __global__ void __launch_bounds__(UPD_THREADS, upd_minb<T>()) k_update(DMesh M, 
                     for (int k = 0; k < 4; k++) out[k] = q0[k] + hh * ((double)k1[k] + Rd[k]);
                 } else {
 #pragma unroll
-                    for (int k = 0; k < 4; k++) out[k] = q0[k] + hh * (double)(k1[k] + R[k]);
+                    for (int k = 0; k < 4; k++) out[k] = q0[k] + hh * to_f64(k1[k] + R[k]);
                 }
             } else if (ST == ST_TVD_1) {
                 if (SPLIT) st4(aux + 4 * (size_t)i, R);
@@ -1182,7 +1202,7 @@ __global__ void __launch_bounds__(UPD_THREADS, upd_minb<T>()) k_update(DMesh M, 
                     T qf[4];
                     ld4(qin + 4 * (size_t)i, qf);
 #pragma unroll
-                    for (int k = 0; k < 4; k++) qfe[k] = (double)qf[k];
+                    for (int k = 0; k < 4; k++) qfe[k] = to_f64(qf[k]);
                 }
 #pragma unroll
                 for (int k = 0; k < 4; k++) out[k] = 0.5 * (q0[k] + qfe[k] + h * Rd[k]);
@@ -1212,13 +1232,13 @@ __global__ void __launch_bounds__(UPD_THREADS, upd_minb<T>()) k_update(DMesh M, 
                     for (int k = 0; k < 4; k++) out[k] = q0[k] + hh * ((double)acc[k] + Rd[k]);
                 } else {
 #pragma unroll
-                    for (int k = 0; k < 4; k++) out[k] = q0[k] + hh * (double)(acc[k] + R[k]);
+                    for (int k = 0; k < 4; k++) out[k] = q0[k] + hh * to_f64(acc[k] + R[k]);
                 }
             }
             if (final_stage) {
                 st4(A.q64 + 4 * (size_t)i, out);
                 if (!is_fp64<T>) {  // the double-float shadow of the solution
-                    T o[4] = {(T)out[0], (T)out[1], (T)out[2], (T)out[3]};
+                    T o[4] = {from_f64<T>(out[0]), from_f64<T>(out[1]), from_f64<T>(out[2]), from_f64<T>(out[3])};
                     st4(qout + 4 * (size_t)i, o);
                 }
 #pragma unroll
@@ -1229,7 +1249,7 @@ __global__ void __launch_bounds__(UPD_THREADS, upd_minb<T>()) k_update(DMesh M, 
                 }
                 bad = isnan(out[0]) || isnan(out[1]) || isnan(out[2]) || isnan(out[3]);
             } else {
-                T o[4] = {(T)out[0], (T)out[1], (T)out[2], (T)out[3]};
+                T o[4] = {from_f64<T>(out[0]), from_f64<T>(out[1]), from_f64<T>(out[2]), from_f64<T>(out[3])};
                 st4(qout + 4 * (size_t)i, o);
             }
         }

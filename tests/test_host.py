@@ -399,6 +399,71 @@ def test_integer_pipe_conversions_match_ieee(tmp_path):
     assert n > 8_000_000 and bad == 0, " ".join(out[:-2])
 
 
+DFLOAT_CHECK = r"""
+#include <cmath>
+#include <cstdio>
+#include <random>
+#include "dfloat.h"
+using ebbdf::df;
+typedef long double L;
+static L val(df a) { return (L)a.hi + (L)a.lo; }
+static std::mt19937_64 rng(11);
+static double u01() { return (rng() >> 11) * 0x1p-53; }
+static df rnd(int emax) {
+    double m = 1.0 + u01();
+    int e = (int)(rng() % (2 * emax + 1)) - emax;
+    double x = std::ldexp(m, e) * ((rng() & 1) ? -1.0 : 1.0);
+    return df(x);
+}
+int main() {
+    const double U = 0x1p-46;
+    double emul = 0, ediv = 0, esqrt = 0, eadd = 0, eaddc = 0, econv = 0, emulf = 0;
+    long n = 0;
+    for (int k = 0; k < 2000000; k++) {
+        df a = rnd(20), b = rnd(20);
+        L va = val(a), vb = val(b);
+        L r;
+        r = va * vb; emul = std::fmax(emul, (double)(std::fabs(val(a * b) - r) / std::fabs(r)) / U);
+        r = va / vb; ediv = std::fmax(ediv, (double)(std::fabs(val(a / b) - r) / std::fabs(r)) / U);
+        float f = b.hi;
+        r = va * (L)f; emulf = std::fmax(emulf, (double)(std::fabs(val(ebbdf::mul_f(a, f)) - r) / std::fabs(r)) / U);
+        df pa = ebbdf::fabs(a);
+        r = std::sqrt(val(pa)); esqrt = std::fmax(esqrt, (double)(std::fabs(val(ebbdf::sqrt(pa)) - r) / r) / U);
+        r = va + vb; eadd = std::fmax(eadd, (double)(std::fabs(val(a + b) - r) / (std::fabs(va) + std::fabs(vb))) / U);
+        // cancellation: b close to -a
+        df c = -(a * df(1.0 + std::ldexp(u01(), -(int)(rng() % 40))));
+        L vc = val(c);
+        r = va + vc; eaddc = std::fmax(eaddc, (double)(std::fabs(val(a + c) - r) / (std::fabs(va) + std::fabs(vc))) / U);
+        double x = std::ldexp(1.0 + u01(), (int)(rng() % 121) - 60) * ((rng() & 1) ? -1.0 : 1.0);
+        econv = std::fmax(econv, (double)(std::fabs(val(df(x)) - (L)x) / std::fabs((L)x)) / U);
+        n++;
+    }
+    std::printf("%ld %.3f %.3f %.3f %.3f %.3f %.3f %.3f\n", n, emul, emulf, ediv, esqrt, eadd, eaddc, econv);
+}
+"""
+
+
+def test_double_float_error_bounds(tmp_path):
+    """The double-float arithmetic of the df precision form (csrc/dfloat.h) against
+    80-bit (x86) or 128-bit (Arm) long double references on 2M random operand pairs
+    over 2^+-20 of both signs: product, product by an FP32 number, quotient and square
+    root within 2 units of 2^-46 of the exact result (relative); sums within 2 units of
+    2^-46 of |a| + |b|, with near-cancelling pairs as well; the conversion from double
+    within 2^-48."""
+    import subprocess
+    src = tmp_path / "dfcheck.cpp"
+    src.write_text(DFLOAT_CHECK)
+    exe = tmp_path / "dfcheck"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", os.path.join(ROOT, "ebbcfd_gb300", "csrc"),
+                    str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    n = int(out[0])
+    emul, emulf, ediv, esqrt, eadd, eaddc, econv = (float(x) for x in out[1:])
+    assert n == 2_000_000
+    assert max(emul, emulf, ediv, esqrt, eadd, eaddc) <= 2.0, out
+    assert econv <= 0.25, out
+
+
 def test_hanging_node_polygons():
     """The non-conforming quad mesh used by the six-neighbour parity case: 14 pentagons
     and one hexagon among the quads, counter-clockwise and tiling the unit square; the
