@@ -1,6 +1,6 @@
 // ebb_solve.cpp -- command-line driver with ebb-solve's interface (app/solver.d:430-470):
 //
-//   ebb-solve -c config.json [-s save_prefix] [--precision fp64|split] [--device N]
+//   ebb-solve -c config.json [-s save_prefix] [--precision fp64|split|df] [--device N]
 //
 // Reads the JSON config and the gmsh mesh it names, runs the time loop of
 // runIntegrator (app/solver.d:38-277) on the GPU through the C ABI, and writes what the
@@ -70,12 +70,23 @@ int main(int argc, char **argv)
             cfg_path = next();
         else if (a == "-s" || a == "--save")
             save_prefix = next();
-        else if (a == "--precision")
-            precision = next() == "split" ? EBB_PREC_SPLIT : EBB_PREC_FP64;
+        else if (a == "--precision") {
+            const std::string p = next();
+            if (p == "fp64")
+                precision = EBB_PREC_FP64;
+            else if (p == "split")
+                precision = EBB_PREC_SPLIT;
+            else if (p == "df")
+                precision = EBB_PREC_DF;
+            else {
+                std::fprintf(stderr, "unknown precision form '%s' (fp64, split or df)\n", p.c_str());
+                return 2;
+            }
+        }
         else if (a == "--device")
             device = std::atoi(next().c_str());
         else {
-            std::fprintf(stderr, "usage: ebb-solve -c config.json [-s save_prefix] [--precision fp64|split] [--device N]\n");
+            std::fprintf(stderr, "usage: ebb-solve -c config.json [-s save_prefix] [--precision fp64|split|df] [--device N]\n");
             return 2;
         }
     }

@@ -8,7 +8,7 @@
  + resident on one GPU.  The command line, the files written and the printed lines are
  + ebb-solve's:
  +
- +     ebb-solve -c config.json [-s save_prefix] [--precision fp64|split] [--device N]
+ +     ebb-solve -c config.json [-s save_prefix] [--precision fp64|split|df] [--device N]
  +
  + writes save_<k>_0.esln every saveIter iterations, final_0.esln and the big-endian
  + (t, drag, lift) triples of boundaryForces.frc; SIGINT/SIGUSR1 stop the loop and
@@ -196,7 +196,7 @@ int main(string[] args)
     int device = 0;
     getopt(args, "c|config", "config file to read", &configFile,
                  "s|save", "Save file to start from", &saveFile,
-                 "precision", "fp64 or split", &precisionName,
+                 "precision", "fp64, split or df", &precisionName,
                  "device", "GPU to run on", &device);
     signal(SIGINT, &handle);
     signal(SIGUSR1, &handle);
@@ -204,8 +204,9 @@ int main(string[] args)
         saveFile ~= "0.esln";
     ebb_set_device(device);
     auto sw = StopWatch(AutoStart.yes);
-    const status = startComputationGpu(readText(configFile), saveFile,
-                                       precisionName == "split" ? EBB_PREC_SPLIT : EBB_PREC_FP64);
+    const precision = precisionName == "split" ? EBB_PREC_SPLIT
+                    : precisionName == "df" ? EBB_PREC_DF : EBB_PREC_FP64;
+    const status = startComputationGpu(readText(configFile), saveFile, precision);
     printf("total run time: %g\n", sw.peek.total!"usecs" / 1e6);
     return status;
 }

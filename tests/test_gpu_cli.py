@@ -98,6 +98,34 @@ def test_ebb_solve_run_and_restart(plate_dir):
     assert fin2["t"] >= d["tEnd"]
 
 
+def test_ebb_solve_precision_forms(plate_dir):
+    """`--precision df` runs the same loop in double-float: the same number of records,
+    times and final state within 1e-9 of the oracle's (relative to each component's
+    largest magnitude).  `--precision split` runs it too (its time steps, from FP32
+    wave speeds, may end the loop one step apart); an unknown form is refused."""
+    B.build()
+    tmp, d = plate_dir
+    conf = gmsh_ref.load_config(json.dumps(d))
+    om = ref.OracleMesh(gmsh_ref.parse_gmsh(str(tmp / "flatPlate_0.msh")), conf)
+    rec = om.run(10 ** 6)
+    qo = om.state()
+    for form in ("df", "split"):
+        p = subprocess.run([B.CLI, "-c", "cfg.json", "--precision", form], cwd=tmp, capture_output=True, text=True,
+                           timeout=300)
+        assert p.returncode == 0, p.stdout + p.stderr
+        frc = read_frc(tmp / "boundaryForces.frc")
+        if form == "split":
+            assert abs(len(frc) - len(rec)) <= 1
+            continue
+        assert len(frc) == len(rec)
+        assert np.abs(frc[:, 0] - rec[:, 0]).max() <= 1e-9 * rec[-1, 0]
+        fin = read_esln(tmp / "final_0.esln")
+        assert (np.abs(fin["q"] - qo).max(axis=0) / np.abs(qo).max(axis=0)).max() <= 1e-9
+    bad = subprocess.run([B.CLI, "-c", "cfg.json", "--precision", "fp16"], cwd=tmp, capture_output=True, text=True,
+                         timeout=60)
+    assert bad.returncode == 2 and "unknown precision form" in bad.stderr
+
+
 def test_ebb_solve_reports_missing_tag(tmp_path):
     B.build()
     shutil.copy(os.path.join(MESHES, "flatPlate_0.msh"), tmp_path / "flatPlate_0.msh")
