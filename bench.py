@@ -202,15 +202,15 @@ def peaks():
 
 
 def profiled_counters(kernel, precision, workload, ncell):
-    """DRAM bytes (read + write) per launch of `kernel` and its FP64-pipe share from the
-    committed ncu summaries under profiles/: lines "traffic: <kernel> <precision>
-    <bytes> <workload> <cells>" and "fp64pipe: <kernel> <precision> <percent>
-    <workload>" (a capture of `cells` cells of the workload; traffic is scaled to
-    `ncell` cells: it grows with the cells processed).  None when no capture covers the
-    kernel."""
+    """DRAM bytes (read + write) per launch of `kernel` and its FP64- and FMA-pipe
+    shares from the committed ncu summaries under profiles/: lines "traffic: <kernel>
+    <precision> <bytes> <workload> <cells>", "fp64pipe: <kernel> <precision> <percent>
+    <workload>" and "fmapipe: ..." alike (a capture of `cells` cells of the workload;
+    traffic is scaled to `ncell` cells: it grows with the cells processed).  None when
+    no capture covers the kernel."""
     import glob
     import re
-    out = {"traffic": None, "fp64_pipe_pct": None}
+    out = {"traffic": None, "fp64_pipe_pct": None, "fma_pipe_pct": None}
     for f in sorted(glob.glob(os.path.join(ROOT, "profiles", "*.md"))):
         for line in open(f):
             m = re.match(r"traffic: (\S+) (\S+) (\d+) (\S+) (\d+)\s*$", line)
@@ -218,9 +218,9 @@ def profiled_counters(kernel, precision, workload, ncell):
                 cells = int(m.group(5))
                 out["traffic"] = {"bytes": int(m.group(3)) * ncell / cells, "source": os.path.relpath(f, ROOT),
                                   "captured_cells": cells}
-            m = re.match(r"fp64pipe: (\S+) (\S+) ([\d.]+) (\S+)\s*$", line)
-            if m and m.group(1) == kernel and m.group(2) == precision and m.group(4) == workload:
-                out["fp64_pipe_pct"] = float(m.group(3))
+            m = re.match(r"(fp64|fma)pipe: (\S+) (\S+) ([\d.]+) (\S+)\s*$", line)
+            if m and m.group(2) == kernel and m.group(3) == precision and m.group(5) == workload:
+                out[m.group(1) + "_pipe_pct"] = float(m.group(4))
     return out
 
 
@@ -330,8 +330,9 @@ def measure(L, E, _lib, mesh, wl, precision, args, local, ws, want_e2e, hist_ste
             row["dram_gbs"] = cnt["traffic"]["bytes"] / sec / 1e9
             row["frac_dram"] = row["dram_gbs"] / peak
             row["traffic_source"] = cnt["traffic"]
-        if cnt["fp64_pipe_pct"] is not None:
-            row["fp64_pipe_active_pct"] = cnt["fp64_pipe_pct"]
+        for pipe in ("fp64", "fma"):
+            if cnt[pipe + "_pipe_pct"] is not None:
+                row[pipe + "_pipe_active_pct"] = cnt[pipe + "_pipe_pct"]
         kernels["k_" + k] = row
     dom = max(("cell", "flux", "update"), key=lambda k: kern_ms[k])
     d = kernels["k_" + dom]
@@ -342,7 +343,8 @@ def measure(L, E, _lib, mesh, wl, precision, args, local, ws, want_e2e, hist_ste
     if precision == "fp64":
         roof["limiter"] = "FP64 pipe (ncu fp64_pipe_active_pct; GB300 runs FP64 at a small fraction of FP32)"
     elif precision == "df":
-        roof["limiter"] = "FP32 pipe (double-float arithmetic: 8-25 FP32 instructions per operation)"
+        roof["limiter"] = ("FP32 (FMA) pipe and instruction issue: double-float arithmetic takes 5-20 FP32 "
+                           "instructions per operation (ncu fma_pipe_active_pct)")
     sol.close()
     return {"value": value, "elapsed": elapsed, "steps": steps_done, "setup_s": setup_s, "roofline": roof,
             "e2e": e2e, "clocks": clk, "state": state, "hist": hist, "status": st, "edge_fluxes": efl}
@@ -901,7 +903,7 @@ def run_serve(args):
                                           % args.seq_steps},
             "sequential_served_form": {"est_total_s": seq32_s, "cell_updates_per_s": cu / seq32_s,
                                        "sample": "split steps at the split path's time per step alone, the rest at "
-                                                 "FP64's"},
+                                                 "the %s form's" % args.finish},
             "throughput_vs_sequential_fp64": (cu / wall) / (cu / seq_s),
             "throughput_vs_sequential_served_form": (cu / wall) / (cu / seq32_s), "bytes_peak": stats["bytes_peak"],
             "error_vs_fp64": err, "mesh_s": round(mesh_s, 1), "clocks": clk}

@@ -288,16 +288,11 @@ int build_instance(const ebb_mesh *mesh, const ebb_config *cfg, InstLayout &L, s
     // time-loop state (app/solver.d:43-50)
     DState &h = L.st0;
     std::memset(&h, 0, sizeof h);
-    h.dt = cfg->dt;
+    set_step(h, cfg->dt);
     h.t = 0;
     h.cfl = cfg->cfl;
     h.cflf = (float)h.cfl;
     h.t_end = cfg->t_end;
-    h.dt_half = h.dt / 2.0;
-    h.dt_sixth = h.dt / 6.0;
-    h.dtf = (float)h.dt;
-    h.dt_half_f = (float)h.dt_half;
-    h.dt_sixth_f = (float)h.dt_sixth;
     h.newdt_bits = 0x7FF0000000000000ull;
     h.rmax_bits = 0;
     h.err_key = EBB_NOERR;

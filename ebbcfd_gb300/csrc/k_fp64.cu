@@ -97,11 +97,7 @@ template <typename T> __global__ void __launch_bounds__(EBB_RED_THREADS) k_step_
                (st->stop_drop > 0 && resid[0] <= st->stop_drop * st->resid_first) ||
                (st->stall_steps > 0 && st->resid_min <= 1e-3 * st->resid_first &&
                 st->iter - st->resid_min_iter > st->stall_steps);
-    st->dt_half = st->dt / 2.0;
-    st->dt_sixth = st->dt / 6.0;
-    st->dtf = (float)st->dt;
-    st->dt_half_f = (float)st->dt_half;
-    st->dt_sixth_f = (float)st->dt_sixth;
+    set_step(*st, st->dt);
     st->newdt_bits = 0x7FF0000000000000ull;  // +inf
     st->rmax_bits = 0ull;
 }

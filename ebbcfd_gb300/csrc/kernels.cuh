@@ -523,6 +523,36 @@ __global__ void __launch_bounds__(cell_threads<T>(), cell_minb<T>()) k_cell(DMes
                 }
             }
         }
+    } else if constexpr (is_df<T>) {
+        // double-float: the neighbour-state gathers in flight before the arithmetic,
+        // which keeps the FP64 path's order (long dependent FP32 sequences leave the
+        // warps waiting on one gather at a time otherwise)
+        int nb[MJ];
+        T qv[MJ][4];
+#pragma unroll
+        for (int j = 0; j < MJ; j++) nb[j] = (j < ne) ? M.s_nbr[(size_t)j * Cs + i] : i;
+#pragma unroll
+        for (int j = 0; j < MJ; j++) ld4(qin + 4 * (size_t)(nb[j] < M.C ? nb[j] : i), qv[j]);
+#pragma unroll
+        for (int j = 0; j < MJ; j++) {
+            if (j < ne) {
+                if (nb[j] >= M.C) {
+                    ghost_state<T>(M, P, st, nb[j] - M.C, qi, qv[j]);
+                    st4(qghost + 4 * (size_t)nb[j], qv[j]);
+                }
+                if (second) {
+                    const typename V2<T>::t gm = ld2<T>(M.g.s_gm, (size_t)j * Cs + i);
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        mn[k] = fmin(mn[k], qv[j][k]);
+                        mx[k] = fmax(mx[k], qv[j][k]);
+                        T du = qv[j][k] - qi[k];
+                        g[k][0] = g[k][0] + gm.x * du;
+                        g[k][1] = g[k][1] + gm.y * du;
+                    }
+                }
+            }
+        }
     } else {
 #pragma unroll
     for (int j = 0; j < MJ; j++) {
@@ -1161,6 +1191,34 @@ __global__ void __launch_bounds__(UPD_THREADS, upd_minb<T>()) k_update(DMesh M, 
                 for (int k = 0; k < 4; k++) o[k] = q32[k] + inc[k];
             }
             st4(qout + 4 * (size_t)i, o);
+        } else if (is_df<T> && !final_stage) {
+            // double-float, a stage before the last: the stage state is the solution's
+            // double-float copy plus the stage increment, all in double-float (it is
+            // stored as one anyway); the FP64 solution is updated by the last stage
+            if constexpr (is_df<T> && (ST == ST_RK2_1 || ST == ST_TVD_1 || ST == ST_RK4_1 || ST == ST_RK4_2 ||
+                                       ST == ST_RK4_3)) {
+                T *aux = reinterpret_cast<T *>(A.aux);
+                T qs[4];
+                ld4(reinterpret_cast<const T *>(A.qs1) + 4 * (size_t)i, qs);
+                T h = st->dtw;
+                if (ST == ST_TVD_1) {
+                    if (P.local_ts) h = cdt[i];
+                } else if (ST == ST_RK2_1 || ST == ST_RK4_1) {
+                    st4(aux + 4 * (size_t)i, R);
+                    if (ST == ST_RK4_1) h = st->dt_half_w;
+                } else {
+                    T acc[4];
+                    ld4(aux + 4 * (size_t)i, acc);
+#pragma unroll
+                    for (int k = 0; k < 4; k++) acc[k] = acc[k] + T(2.0f) * R[k];
+                    st4(aux + 4 * (size_t)i, acc);
+                    if (ST == ST_RK4_2) h = st->dt_half_w;
+                }
+                T o[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) o[k] = qs[k] + h * R[k];
+                st4(qout + 4 * (size_t)i, o);
+            }
         } else {
             T *aux = reinterpret_cast<T *>(A.aux);
             double q0[4], Rd[4], out[4];

@@ -95,7 +95,22 @@ struct DState {
                                        // new minimum for this many iterations (a stalled solve)
     int64_t resid_min_iter;            // iteration of the smallest density residual so far
     double resid_min;                  // that residual
+    ebbdf::df dtw, dt_half_w;          // double-float copies (the df path's stage states)
 };
+
+// dt and what is derived from it: the halves and sixths of the RK stages and their FP32
+// (split path) and double-float (df path) copies
+EBB_DF_HD void set_step(DState &h, double dt)
+{
+    h.dt = dt;
+    h.dt_half = dt / 2.0;
+    h.dt_sixth = dt / 6.0;
+    h.dtf = (float)dt;
+    h.dt_half_f = (float)h.dt_half;
+    h.dt_sixth_f = (float)h.dt_sixth;
+    h.dtw = ebbdf::df(dt);
+    h.dt_half_w = ebbdf::df(h.dt_half);
+}
 
 // record layout matches ebb_step_record
 struct DRecord {

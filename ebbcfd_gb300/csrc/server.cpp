@@ -131,12 +131,7 @@ void worker(ebb_server *sv)
                 for (int64_t i = 0; i < r->L.C; i++)
                     for (int c = 0; c < 4; c++) r->L.q[4 * i + c] = r->resume_q[4 * (size_t)r->L.perm[i] + c];
                 h.t = r->resume.t;
-                h.dt = r->resume.dt;
-                h.dt_half = h.dt / 2.0;
-                h.dt_sixth = h.dt / 6.0;
-                h.dtf = (float)h.dt;
-                h.dt_half_f = (float)h.dt_half;
-                h.dt_sixth_f = (float)h.dt_sixth;
+                set_step(h, r->resume.dt);
                 h.cfl = r->resume.cfl;
                 h.cflf = (float)h.cfl;
                 h.iter = r->resume.iterations;

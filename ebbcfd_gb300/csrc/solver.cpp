@@ -460,12 +460,7 @@ int ebb_set_time(ebb_solver *s, double t, double dt)
     int r = solver_sync_state(s, h);
     if (r) return r;
     h.t = t;
-    h.dt = dt;
-    h.dt_half = dt / 2.0;
-    h.dt_sixth = dt / 6.0;
-    h.dtf = (float)dt;
-    h.dt_half_f = (float)h.dt_half;
-    h.dt_sixth_f = (float)h.dt_sixth;
+    set_step(h, dt);
     h.done = !(h.t < h.t_end);
     return solver_write_state(s, h);
 }
@@ -521,12 +516,7 @@ int ebb_step(ebb_solver *s, double *dt, double *rmax)
     int r = solver_sync_state(s, h);
     if (r) return r;
     const int saved_done = h.done;
-    h.dt = *dt;
-    h.dt_half = *dt / 2.0;
-    h.dt_sixth = *dt / 6.0;
-    h.dtf = (float)*dt;
-    h.dt_half_f = (float)h.dt_half;
-    h.dt_sixth_f = (float)h.dt_sixth;
+    set_step(h, *dt);
     h.newdt_bits = 0x7FF0000000000000ull;
     h.rmax_bits = (*rmax > 0) ? dbits(*rmax) : 0ull;
     h.done = 0;

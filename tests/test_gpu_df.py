@@ -70,14 +70,12 @@ def test_df_hundred_steps(name):
     assert rel_err(s.state, om.state()) <= DF_STATE_TOL, rel_err(s.state, om.state())
     assert rel_err(rec_d[:, [0, 8]], rec_o[:, [0, 8]]) <= 1e-10
     # Each residual column is normalised by the sum of its state component over the
-    # cells (app/solver.d); where that sum cancels to a small fraction of the summed
-    # magnitudes (the cross-stream momentum of a flow along the x axis) the column's
-    # value is dominated by the cancellation, in the oracle as in any other arithmetic,
-    # and is not compared.
-    qf = om.state()
-    cond = np.abs(qf.sum(axis=0)) / np.maximum(np.abs(qf).sum(axis=0), 1e-300)
-    cols = [3 + k for k in range(4) if cond[k] > 1e-6]
-    assert 3 in cols and 6 in cols
+    # cells (app/solver.d).  Density and energy are positive, so their sums never
+    # cancel; a momentum sum that crosses zero during the run (the oracle's column
+    # changes sign: the cross-stream momentum of a flow along the x axis) makes the
+    # column's value a ratio to a cancelled sum, dominated by the cancellation in the
+    # oracle as in any other arithmetic, and that column is not compared.
+    cols = [3, 6] + [k for k in (4, 5) if np.all(rec_o[:, k] > 0) or np.all(rec_o[:, k] < 0)]
     assert rel_err(rec_d[:, cols], rec_o[:, cols]) <= DF_HIST_TOL
     fscale = max(np.abs(rec_o[:, 1:3]).max(), 1.0)
     assert np.abs(rec_d[:, 1:3] - rec_o[:, 1:3]).max() <= DF_HIST_TOL * fscale
