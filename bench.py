@@ -465,7 +465,8 @@ def mms32_config():
 def run_mms32(args):
     """32x32 quads on [0,1]^2, the sine manufactured fields, Dirichlet boundaries, Roe,
     limited, TVD-RK2, CFL 0.5, 1000 steps: L2(rho) error vs the exact field for the
-    oracle, the plain FP64 path (which must equal it bitwise) and the split path."""
+    oracle, the plain FP64 path (which must equal it bitwise), the split path and the
+    double-float path."""
     import ctypes as C
     import ebbcfd_gb300 as E
     from ebbcfd_gb300 import _lib, meshgen
@@ -475,7 +476,7 @@ def run_mms32(args):
     steps = args.steps if args.steps_given else 1000
     out = {"workload": "mms32-sine-roe-tvd-cfl0.5", "cells": 1024, "steps": steps}
     q_exact, _, _ = ref.mms_eval(2, gen.to_solver_mesh().centroids())
-    for prec in ("fp64", "split"):
+    for prec in ("fp64", "split", "df"):
         cfg = E.load_config(mms32_config())
         cfg.mms = 2
         sol = E.UfvmSolver(gen.to_solver_mesh(), cfg, precision=prec)
@@ -490,8 +491,11 @@ def run_mms32(args):
     qo = om.state()
     out["oracle"] = {"l2_rho": float(np.sqrt(np.mean((qo[:, 0] - q_exact[:, 0]) ** 2)))}
     out["fp64_equals_oracle_bitwise"] = bool(np.array_equal(out["fp64"]["state"], qo))
-    out["split_l2_rel_diff"] = abs(out["split"]["l2_rho"] / out["fp64"]["l2_rho"] - 1)
-    for prec in ("fp64", "split"):
+    for prec in ("split", "df"):
+        out[prec + "_l2_rel_diff"] = abs(out[prec]["l2_rho"] / out["fp64"]["l2_rho"] - 1)
+        out[prec + "_state_max_rel_err"] = float((np.abs(out[prec]["state"] - qo).max(axis=0)
+                                                  / np.abs(qo).max(axis=0)).max())
+    for prec in ("fp64", "split", "df"):
         del out[prec]["state"]
     return out
 
@@ -533,9 +537,10 @@ def theory_shock_angle(M=2.5, theta_deg=15.0, g=1.4):
 def run_wedge5000(args):
     """Accuracy of configuration 2: the 1M-cell Mach 2.5 wedge run 5000 RK2 steps in
     plain FP64 (bitwise equal to the oracle on the parity cases, and used here as the
-    reference solution: the oracle would take ~7 min on the host) and in split
-    precision; shock angle of both against the oblique-shock relation, and the split
-    path's L2 state error against FP64."""
+    reference solution: the oracle would take ~7 min on the host), in split precision
+    and in double-float; shock angle of each against the oblique-shock relation, and
+    the split and double-float paths' state, drag and lift errors against FP64 (forces
+    on the ramp)."""
     import ctypes as C
     import ebbcfd_gb300 as E
     from ebbcfd_gb300 import _lib, meshgen
@@ -545,8 +550,8 @@ def run_wedge5000(args):
     xy = mesh.centroids()
     out = {"workload": "wedge-M2.5-rusanov-rk2-cfl0.4-accuracy", "cells": mesh.n_cells, "steps": steps,
            "theory_shock_angle_deg": theory_shock_angle()}
-    qs = {}
-    for prec in ("fp64", "split"):
+    qs, forces = {}, {}
+    for prec in ("fp64", "split", "df"):
         s = E.UfvmSolver(mesh, E.load_config(wedge_config()), precision=prec)
         n = C.c_int64()
         ms = C.c_double()
@@ -555,17 +560,24 @@ def run_wedge5000(args):
             s._raise(code)
         q = s.state
         qs[prec] = q
+        st = s.status()[0]
+        forces[prec] = (st["drag"], st["lift"])
         t_end = s.time()[0]
         # the corner shock is established within about the distance the flow has moved
         span = min(1.1, 0.9 * t_end)
         beta, x0 = shock_angle(xy, q, x_lo=0.5 + 0.15 * span, x_hi=0.5 + 0.85 * span, nbins=10)
         out[prec] = {"cell_updates_per_s": mesh.n_cells * n.value / (ms.value / 1e3), "shock_angle_deg": beta,
-                     "shock_origin_x": x0, "t": t_end, "shock_window_x": [0.5 + 0.15 * span, 0.5 + 0.85 * span]}
+                     "shock_origin_x": x0, "t": t_end, "shock_window_x": [0.5 + 0.15 * span, 0.5 + 0.85 * span],
+                     "drag": st["drag"], "lift": st["lift"]}
         s.close()
-    d = qs["split"] - qs["fp64"]
-    out["split_l2_rel_err"] = [float(np.sqrt(np.mean(d[:, k] ** 2)) / np.sqrt(np.mean(qs["fp64"][:, k] ** 2)))
-                               for k in range(4)]
-    out["split_max_rel_err"] = float((np.abs(d).max(axis=0) / np.abs(qs["fp64"]).max(axis=0)).max())
+    d64, l64 = forces["fp64"]
+    for prec in ("split", "df"):
+        d = qs[prec] - qs["fp64"]
+        out[prec + "_l2_rel_err"] = [float(np.sqrt(np.mean(d[:, k] ** 2)) / np.sqrt(np.mean(qs["fp64"][:, k] ** 2)))
+                                     for k in range(4)]
+        out[prec + "_max_rel_err"] = float((np.abs(d).max(axis=0) / np.abs(qs["fp64"]).max(axis=0)).max())
+        out[prec + "_drag_rel_err"] = abs(forces[prec][0] - d64) / abs(d64)
+        out[prec + "_lift_rel_err"] = abs(forces[prec][1] - l64) / abs(l64)
     return out
 
 

@@ -492,9 +492,10 @@ def test_hanging_node_polygons():
 
 def test_bench_roofline_inputs():
     """bench.py's roofline inputs: the committed ncu summaries carry DRAM traffic for
-    every stage kernel of both precision forms on the wedge (scaled by cell count),
-    the FP64 kernels' FP64-pipe share, and the algorithmic-bytes model counts the split
-    update's freestream-correction reads and the viscous gradient traffic."""
+    every stage kernel of both precision forms on the wedge and of all three on the
+    plate (scaled by cell count), the FP64 kernels' FP64-pipe share and the
+    double-float kernels' FMA-pipe share, and the algorithmic-bytes model counts the
+    split update's freestream-correction reads and the viscous gradient traffic."""
     import sys
     sys.path.insert(0, ROOT)
     import bench
@@ -507,6 +508,13 @@ def test_bench_roofline_inputs():
             assert abs(half["bytes"] - t["bytes"] * (cells // 2) / cells) <= 1.0
         assert bench.profiled_counters(kern, "fp64", wl, cells)["fp64_pipe_pct"] > 50
     assert bench.profiled_counters("k_flux", "fp64", "no-such-workload", cells)["traffic"] is None
+    # the headline plate: every kernel of the three forms, and the double-float kernels'
+    # FMA-pipe share
+    for kern in ("k_cell", "k_flux", "k_update"):
+        for prec in ("fp64", "split", "df"):
+            t = bench.profiled_counters(kern, prec, bench.PLATE_WORKLOAD, 1001778)["traffic"]
+            assert t is not None and t["bytes"] > 1e8 and t["captured_cells"] == 1001778, (kern, prec)
+        assert bench.profiled_counters(kern, "df", bench.PLATE_WORKLOAD, 1001778)["fma_pipe_pct"] > 10
 
     class Info:
         n_cells, face_slots, n_int_edges, n_ghost = 1000, 3000, 1480, 40
