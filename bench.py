@@ -546,7 +546,7 @@ def run_wedge5000(args):
     from ebbcfd_gb300 import _lib, meshgen
     L = _lib.load()
     steps = args.steps if args.steps_given else 5000
-    mesh = meshgen.wedge(args.cells, seed=0).to_solver_mesh()
+    mesh = meshgen.wedge(args.cells if args.cells_given else WORKLOADS["wedge"]["cells"], seed=0).to_solver_mesh()
     xy = mesh.centroids()
     out = {"workload": "wedge-M2.5-rusanov-rk2-cfl0.4-accuracy", "cells": mesh.n_cells, "steps": steps,
            "theory_shock_angle_deg": theory_shock_angle()}

@@ -77,6 +77,31 @@ template <> __device__ __forceinline__ double half<double>(double x)
 }
 template <> __device__ __forceinline__ df half<df>(df x) { return df(0.5f * x.hi, 0.5f * x.lo); }
 
+// 0 + x, the start of the reference's matrix-vector sums (numd Matrix * Vector adds
+// each product to a zero).  It is x except that -0 becomes +0 (NaN stays NaN).  FP64:
+// that rule on the bit pattern, on the integer pipe.
+template <typename T> __device__ __forceinline__ T zero_plus(T x) { return T(0.0) + x; }
+template <> __device__ __forceinline__ double zero_plus<double>(double x)
+{
+    return __double_as_longlong(x) == (long long)0x8000000000000000ull ? 0.0 : x;
+}
+template <> __device__ __forceinline__ df zero_plus<df>(df x) { return x.hi == 0.0f ? df(0.0f, 0.0f) : x; }
+
+// 0 nx + 0 ny: a signed zero, -0 when both products are -0 (nx and ny negative), and
+// NaN when nx or ny is infinite or NaN.  FP64: the signs on the integer pipe for finite
+// normals (a warp holding a non-finite one takes the FP64 expression).
+template <typename T> __device__ __forceinline__ T zero_dot(T nx, T ny) { return T(0.0) * nx + T(0.0) * ny; }
+template <> __device__ __forceinline__ double zero_dot<double>(double nx, double ny)
+{
+    const int hx = __double2hiint(nx), hy = __double2hiint(ny);
+    const bool fin = ((hx & 0x7ff00000) != 0x7ff00000) && ((hy & 0x7ff00000) != 0x7ff00000);
+    double z = (hx < 0 && hy < 0) ? -0.0 : 0.0;
+    if (__any_sync(__activemask(), !fin)) {
+        if (!fin) z = 0.0 * nx + 0.0 * ny;
+    }
+    return z;
+}
+
 template <typename T> __device__ __forceinline__ T dsqrt(T x) { return sqrt(x); }
 template <> __device__ __forceinline__ float dsqrt<float>(float x) { return sqrtf(x); }
 template <typename T> __device__ __forceinline__ T dpow(T x, T y) { return pow(x, y); }
@@ -407,13 +432,13 @@ __device__ __forceinline__ void diffusive_flux(const ViscConst<T> &vc, T mu, con
     const T x0 = dq[0][0], x1 = dq[1][0], x2 = dq[2][0], x3 = dq[3][0];
     const T y0 = dq[0][1], y1 = dq[1][1], y2 = dq[2][1], y3 = dq[3][1];
     // matrix-vector products accumulate left to right from 0 (numd Matrix * Vector)
-    T G0_1 = (T(0.0) + a10 * x0 + a11 * x1) + (T(0.0) + b10 * y0 + b12 * y2);
-    T G0_2 = (T(0.0) + a20 * x0 + a22 * x2) + (T(0.0) + b20 * y0 + b21 * y1);
-    T G0_3 = (T(0.0) + a30 * x0 + a31 * x1 + a32 * x2 + a33 * x3) + (T(0.0) + b30 * y0 + b31 * y1 + b32 * y2);
-    T G1_1 = (T(0.0) + c10 * x0 + c12 * x2) + (T(0.0) + d10 * y0 + d11 * y1);
-    T G1_2 = (T(0.0) + c20 * x0 + c22 * x2) + (T(0.0) + d20 * y0 + d22 * y2);
-    T G1_3 = (T(0.0) + c30 * x0 + c31 * x1 + c32 * x2) + (T(0.0) + d30 * y0 + d31 * y1 + d32 * y2 + d33 * y3);
-    out[0] = T(0.0) * nx + T(0.0) * ny;
+    T G0_1 = (zero_plus(a10 * x0) + a11 * x1) + (zero_plus(b10 * y0) + b12 * y2);
+    T G0_2 = (zero_plus(a20 * x0) + a22 * x2) + (zero_plus(b20 * y0) + b21 * y1);
+    T G0_3 = (zero_plus(a30 * x0) + a31 * x1 + a32 * x2 + a33 * x3) + (zero_plus(b30 * y0) + b31 * y1 + b32 * y2);
+    T G1_1 = (zero_plus(c10 * x0) + c12 * x2) + (zero_plus(d10 * y0) + d11 * y1);
+    T G1_2 = (zero_plus(c20 * x0) + c22 * x2) + (zero_plus(d20 * y0) + d22 * y2);
+    T G1_3 = (zero_plus(c30 * x0) + c31 * x1 + c32 * x2) + (zero_plus(d30 * y0) + d31 * y1 + d32 * y2 + d33 * y3);
+    out[0] = zero_dot(nx, ny);
     out[1] = G0_1 * nx + G1_1 * ny;
     out[2] = G0_2 * nx + G1_2 * ny;
     out[3] = G0_3 * nx + G1_3 * ny;
