@@ -16,7 +16,10 @@ parallel).  Each variant's kernels of the three precision forms are timed with
 ebb_profile_kernels (CUDA events on the solver stream, best of three rounds) on the
 headline workload -- the 4.0M-cell Navier-Stokes plate (--workload wedge: the 1.0M
 Mach 2.5 wedge) -- and per kernel the fastest setting over the rows is kept.  The
-kernels are independent launches, so one variant measures all nine at once.  Register
+kernels are independent launches, so one variant measures all of them at once.  Split
+precision has two launch-shape profiles: viscous meshes (gradients stored, the
+viscous flux) take the shapes timed on the tuned workload, inviscid meshes their own,
+timed on the wedge.  Register
 allocation and block size change no FP64 result bit (the kernels stay bitwise equal to
 the oracle); the update block size changes the order of the RMS residual sums only.
 
@@ -47,14 +50,24 @@ CANDIDATES = {
     "df": {"cell": [(128, 2), (128, 1), (128, 3), (256, 1), (256, 2), (64, 4), (64, 6)],
            "flux": [(128, 2), (128, 1), (128, 3), (256, 1), (256, 2), (64, 4), (64, 6)],
            "update": [3, 1, 2, 2, 1, 4, 1]},
+    # split precision on inviscid meshes (its own launch-shape profile, timed on the wedge)
+    "split_inv": {"cell": [(128, 8), (128, 10), (128, 6), (256, 4), (256, 3), (64, 16), (64, 12)],
+                  "flux": [(128, 12), (128, 10), (128, 8), (256, 6), (256, 4), (64, 20), (64, 16)],
+                  "update": [8, 6, 4, 4, 3, 8, 2]},
 }
+# the form each candidate set is built and timed in, and on which workload (None: the
+# workload being tuned for)
+FORM = {"split": ("split", None), "fp64": ("fp64", None), "df": ("df", None), "split_inv": ("split", "wedge")}
 UPD_TB = [256, 256, 256, 512, 512, 256, 512]
 N_ROWS = len(UPD_TB)
 MACRO = {("split", "cell"): ("EBB_CELL_TB_F", "EBB_CELL_MINB_F"), ("split", "flux"): ("EBB_FLUX_TB_F", "EBB_FLUX_MINB_F"),
          ("fp64", "cell"): ("EBB_CELL_TB_D", "EBB_CELL_MINB_D"), ("fp64", "flux"): ("EBB_FLUX_TB_D", "EBB_FLUX_MINB_D"),
          ("df", "cell"): ("EBB_CELL_TB_W", "EBB_CELL_MINB_W"), ("df", "flux"): ("EBB_FLUX_TB_W", "EBB_FLUX_MINB_W"),
          ("split", "update"): ("EBB_UPD_TB", "EBB_UPD_MINB_F"), ("fp64", "update"): ("EBB_UPD_TB", "EBB_UPD_MINB_D"),
-         ("df", "update"): ("EBB_UPD_TB", "EBB_UPD_MINB_W")}
+         ("df", "update"): ("EBB_UPD_TB", "EBB_UPD_MINB_W"),
+         ("split_inv", "cell"): ("EBB_CELL_TB_FI", "EBB_CELL_MINB_FI"),
+         ("split_inv", "flux"): ("EBB_FLUX_TB_FI", "EBB_FLUX_MINB_FI"),
+         ("split_inv", "update"): ("EBB_UPD_TB", "EBB_UPD_MINB_FI")}
 
 
 def setting(row):
@@ -101,16 +114,20 @@ def _measure(row, workload, cells):
     sys.path.insert(0, ROOT)
     import bench
     L = _lib.load(build_if_missing=False)
-    wl = bench.WORKLOADS[workload]
-    mesh = bench.make_mesh(workload, cells or wl["cells"]).to_solver_mesh()
+    meshes = {}
     us = {}
     for p in CANDIDATES:
-        s = E.UfvmSolver(mesh, E.load_config(wl["config"]()), p)
+        prec, wname = FORM[p]
+        wname = wname or workload
+        wl = bench.WORKLOADS[wname]
+        if wname not in meshes:
+            meshes[wname] = bench.make_mesh(wname, cells if wname == workload and cells else wl["cells"]).to_solver_mesh()
+        s = E.UfvmSolver(meshes[wname], E.load_config(wl["config"]()), prec)
         s.run(5, records=False)
         ms = (C.c_double * 4)()
         best = None
         for _ in range(3):
-            if L.ebb_profile_kernels(s.h, {"split": 20, "df": 6, "fp64": 3}[p], ms):
+            if L.ebb_profile_kernels(s.h, {"split": 20, "df": 6, "fp64": 3}[prec], ms):
                 raise RuntimeError("profiling failed")
             best = list(ms) if best is None else [min(a, b) for a, b in zip(best, ms)]
         s.close()
@@ -161,7 +178,7 @@ def tune(workload="plate", cells=None, out=None):
              (tb_upd, ", ".join("%d: %.1f us" % kv for kv in sorted(upd.items()))), "#pragma once"]
     for (p, k), (mt, mb) in MACRO.items():
         tb, b = choice[(p, k)]
-        if k != "update" or p == "split":
+        if k != "update" or p == "split":  # one update block size (EBB_UPD_TB) for all
             text += ["#ifndef %s" % mt, "#define %s %d" % (mt, tb), "#endif"]
         text += ["#ifndef %s" % mb, "#define %s %d" % (mb, b), "#endif"]
     path = out or os.path.join(HERE, "csrc", "tuned.h")

@@ -47,7 +47,26 @@ constexpr int ERR_NAN_EDGE = 8, ERR_NAN_CELL = 9, ERR_BC = 11;
 #include "tuned.h"
 constexpr int UPD_THREADS = EBB_UPD_TB;
 static_assert(EBB_UPD_TB == 256 || EBB_UPD_TB == 512, "k_update's block reductions take 256 or 512 threads");
-// launch shapes per arithmetic type: _F split (float), _D plain FP64, _W double-float
+// Launch shapes per arithmetic type and profile: _F split (float) on viscous meshes
+// (tuned on the Navier-Stokes plate), _FI split on inviscid meshes (tuned on the Euler
+// wedge: no stored gradients, fewer live values), _D plain FP64, _W double-float.  The
+// profile PR (0 viscous or other forms, 1 split inviscid) is a template parameter of the
+// stage kernels because the register cap is a compile-time launch bound.
+#ifndef EBB_CELL_TB_FI
+#define EBB_CELL_TB_FI 128
+#endif
+#ifndef EBB_CELL_MINB_FI
+#define EBB_CELL_MINB_FI 8
+#endif
+#ifndef EBB_FLUX_TB_FI
+#define EBB_FLUX_TB_FI 128
+#endif
+#ifndef EBB_FLUX_MINB_FI
+#define EBB_FLUX_MINB_FI 12
+#endif
+#ifndef EBB_UPD_MINB_FI
+#define EBB_UPD_MINB_FI 8
+#endif
 #ifndef EBB_CELL_TB_W
 #define EBB_CELL_TB_W 128
 #endif
@@ -63,40 +82,43 @@ static_assert(EBB_UPD_TB == 256 || EBB_UPD_TB == 512, "k_update's block reductio
 #ifndef EBB_UPD_MINB_W
 #define EBB_UPD_MINB_W 3
 #endif
-template <typename T> constexpr int pick(int f, int d, int w)
+template <typename T, int PR> constexpr int pick(int f, int fi, int d, int w)
 {
-    return std::is_same<T, float>::value ? f : (std::is_same<T, double>::value ? d : w);
+    return std::is_same<T, float>::value ? (PR ? fi : f) : (std::is_same<T, double>::value ? d : w);
 }
-template <typename T> constexpr int cell_threads() { return pick<T>(EBB_CELL_TB_F, EBB_CELL_TB_D, EBB_CELL_TB_W); }
-template <typename T> constexpr int flux_threads() { return pick<T>(EBB_FLUX_TB_F, EBB_FLUX_TB_D, EBB_FLUX_TB_W); }
-template <typename T> constexpr int cell_minb() { return pick<T>(EBB_CELL_MINB_F, EBB_CELL_MINB_D, EBB_CELL_MINB_W); }
-template <typename T> constexpr int flux_minb() { return pick<T>(EBB_FLUX_MINB_F, EBB_FLUX_MINB_D, EBB_FLUX_MINB_W); }
-template <typename T> constexpr int upd_minb() { return pick<T>(EBB_UPD_MINB_F, EBB_UPD_MINB_D, EBB_UPD_MINB_W); }
+template <typename T, int PR> constexpr int cell_threads()
+{
+    return pick<T, PR>(EBB_CELL_TB_F, EBB_CELL_TB_FI, EBB_CELL_TB_D, EBB_CELL_TB_W);
+}
+template <typename T, int PR> constexpr int flux_threads()
+{
+    return pick<T, PR>(EBB_FLUX_TB_F, EBB_FLUX_TB_FI, EBB_FLUX_TB_D, EBB_FLUX_TB_W);
+}
+template <typename T, int PR> constexpr int cell_minb()
+{
+    return pick<T, PR>(EBB_CELL_MINB_F, EBB_CELL_MINB_FI, EBB_CELL_MINB_D, EBB_CELL_MINB_W);
+}
+template <typename T, int PR> constexpr int flux_minb()
+{
+    return pick<T, PR>(EBB_FLUX_MINB_F, EBB_FLUX_MINB_FI, EBB_FLUX_MINB_D, EBB_FLUX_MINB_W);
+}
+template <typename T, int PR> constexpr int upd_minb()
+{
+    return pick<T, PR>(EBB_UPD_MINB_F, EBB_UPD_MINB_FI, EBB_UPD_MINB_D, EBB_UPD_MINB_W);
+}
 // an SM holds at most 2048 threads: every (threads, minimum blocks) pair must fit
-static_assert(EBB_CELL_TB_F * EBB_CELL_MINB_F <= 2048 && EBB_CELL_TB_D * EBB_CELL_MINB_D <= 2048, "k_cell bounds");
-static_assert(EBB_FLUX_TB_F * EBB_FLUX_MINB_F <= 2048 && EBB_FLUX_TB_D * EBB_FLUX_MINB_D <= 2048, "k_flux bounds");
-static_assert(EBB_UPD_TB * EBB_UPD_MINB_F <= 2048 && EBB_UPD_TB * EBB_UPD_MINB_D <= 2048, "k_update bounds");
+static_assert(EBB_CELL_TB_F * EBB_CELL_MINB_F <= 2048 && EBB_CELL_TB_D * EBB_CELL_MINB_D <= 2048 &&
+                  EBB_CELL_TB_FI * EBB_CELL_MINB_FI <= 2048,
+              "k_cell bounds");
+static_assert(EBB_FLUX_TB_F * EBB_FLUX_MINB_F <= 2048 && EBB_FLUX_TB_D * EBB_FLUX_MINB_D <= 2048 &&
+                  EBB_FLUX_TB_FI * EBB_FLUX_MINB_FI <= 2048,
+              "k_flux bounds");
+static_assert(EBB_UPD_TB * EBB_UPD_MINB_F <= 2048 && EBB_UPD_TB * EBB_UPD_MINB_D <= 2048 &&
+                  EBB_UPD_TB * EBB_UPD_MINB_FI <= 2048,
+              "k_update bounds");
 static_assert(EBB_CELL_TB_W * EBB_CELL_MINB_W <= 2048 && EBB_FLUX_TB_W * EBB_FLUX_MINB_W <= 2048 &&
                   EBB_UPD_TB * EBB_UPD_MINB_W <= 2048,
               "double-float bounds");
-#ifndef EBB_CELL_MINB_F
-#define EBB_CELL_MINB_F 12
-#endif
-#ifndef EBB_FLUX_MINB_F
-#define EBB_FLUX_MINB_F 16
-#endif
-#ifndef EBB_UPD_MINB_F
-#define EBB_UPD_MINB_F 8
-#endif
-#ifndef EBB_CELL_MINB_D
-#define EBB_CELL_MINB_D 1
-#endif
-#ifndef EBB_FLUX_MINB_D
-#define EBB_FLUX_MINB_D 1
-#endif
-#ifndef EBB_UPD_MINB_D
-#define EBB_UPD_MINB_D 1
-#endif
 
 
 // Viscosity, Prandtl and CFL numbers in the arithmetic type: the split kernels read
@@ -453,8 +475,8 @@ __device__ __forceinline__ void lp_limit(const DMesh &M, int i, int ne, const T 
     }
 }
 
-template <typename T, int MJ, bool LP, bool UNI>
-__global__ void __launch_bounds__(cell_threads<T>(), cell_minb<T>()) k_cell(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, int limit)
+template <typename T, int MJ, bool LP, bool UNI, int PR>
+__global__ void __launch_bounds__(cell_threads<T, PR>(), cell_minb<T, PR>()) k_cell(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, int limit)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool act = i < M.C;
@@ -877,8 +899,8 @@ __device__ void boundary_flux(const DMesh &M, const DPhys &P, const DArrays &A, 
     reinterpret_cast<T *>(A.fs)[e] = len * sMax;
 }
 
-template <typename T>
-__global__ void __launch_bounds__(flux_threads<T>(), flux_minb<T>()) k_flux(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, int nbi)
+template <typename T, int PR>
+__global__ void __launch_bounds__(flux_threads<T, PR>(), flux_minb<T, PR>()) k_flux(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, int nbi)
 {
     if ((int)blockIdx.x >= nbi) {
         grid_dep_release();
@@ -971,8 +993,8 @@ __device__ __forceinline__ float warp_maxf(float v)
 // FP64 for both precision forms.  FP64 path: qin/qout are double stage states as in
 // integrators.d.  Split path: qin is the FP32 stage input, q64 is updated in FP64 and
 // the next stage input (qout) is its FP32 rounding.
-template <typename T, int ST, int MJ, bool UNI>
-__global__ void __launch_bounds__(UPD_THREADS, upd_minb<T>()) k_update(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, T *qout,
+template <typename T, int ST, int MJ, bool UNI, int PR>
+__global__ void __launch_bounds__(UPD_THREADS, upd_minb<T, PR>()) k_update(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, T *qout,
                                                        int dt_update, int need_dt, int final_stage)
 {
     constexpr bool SPLIT = sizeof(T) == 4;
@@ -1419,10 +1441,10 @@ __global__ void __launch_bounds__(UPD_THREADS, upd_minb<T>()) k_update(DMesh M, 
 
 inline int ret(cudaError_t e) { return e == cudaSuccess ? 0 : (int)e; }
 
-template <typename T>
-int launch_cell_impl(const DMesh &M, const DPhys &P, const DArrays &A, const T *qin, int limit, void *stream)
+template <typename T, int PR>
+int launch_cell_pr(const DMesh &M, const DPhys &P, const DArrays &A, const T *qin, int limit, void *stream)
 {
-    const int TB = cell_threads<T>();
+    const int TB = cell_threads<T, PR>();
     dim3 grid((M.C + TB - 1) / TB);
     if (grid.x == 0) return 0;
     cudaStream_t s = (cudaStream_t)stream;
@@ -1430,9 +1452,9 @@ int launch_cell_impl(const DMesh &M, const DPhys &P, const DArrays &A, const T *
     cudaError_t e;
 #define EBB_CELL_U(MJ, U)                                                                 \
     if (lp)                                                                               \
-        e = launch_dep(k_cell<T, MJ, true, U>, grid, dim3(TB), s, M, P, A, qin, limit);  \
+        e = launch_dep(k_cell<T, MJ, true, U, PR>, grid, dim3(TB), s, M, P, A, qin, limit); \
     else                                                                                  \
-        e = launch_dep(k_cell<T, MJ, false, U>, grid, dim3(TB), s, M, P, A, qin, limit);
+        e = launch_dep(k_cell<T, MJ, false, U, PR>, grid, dim3(TB), s, M, P, A, qin, limit);
 #define EBB_CELL(MJ)           \
     if (M.uniform) {           \
         EBB_CELL_U(MJ, true)   \
@@ -1451,27 +1473,28 @@ int launch_cell_impl(const DMesh &M, const DPhys &P, const DArrays &A, const T *
     return ret(e);
 }
 
-template <typename T> int launch_flux_impl(const DMesh &M, const DPhys &P, const DArrays &A, const T *qin, void *stream)
+template <typename T, int PR>
+int launch_flux_pr(const DMesh &M, const DPhys &P, const DArrays &A, const T *qin, void *stream)
 {
-    const int TB = flux_threads<T>();
+    const int TB = flux_threads<T, PR>();
     int nbi = (M.Eint + TB - 1) / TB, nbb = (M.G + TB - 1) / TB;
     if (nbi + nbb == 0) return 0;
-    return ret(launch_dep(k_flux<T>, dim3(nbi + nbb), dim3(TB), (cudaStream_t)stream, M, P, A, qin, nbi));
+    return ret(launch_dep(k_flux<T, PR>, dim3(nbi + nbb), dim3(TB), (cudaStream_t)stream, M, P, A, qin, nbi));
 }
 
-template <typename T>
-int launch_update_impl(const DMesh &M, const DPhys &P, const DArrays &A, int stage, const T *qin, T *qout,
-                       int dt_update, int need_dt, int final_stage, void *stream)
+template <typename T, int PR>
+int launch_update_pr(const DMesh &M, const DPhys &P, const DArrays &A, int stage, const T *qin, T *qout,
+                     int dt_update, int need_dt, int final_stage, void *stream)
 {
     dim3 grid(M.n_upd_blocks);
     if (grid.x == 0) return 0;
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e = cudaSuccess;
 #define EBB_UPD_MJ(S, MJ)                                                                                         \
-    e = M.uniform ? launch_dep(k_update<T, S, MJ, true>, grid, dim3(UPD_THREADS), s, M, P, A, qin, qout, dt_update,  \
-                               need_dt, final_stage)                                                                 \
-                  : launch_dep(k_update<T, S, MJ, false>, grid, dim3(UPD_THREADS), s, M, P, A, qin, qout, dt_update, \
-                               need_dt, final_stage)
+    e = M.uniform ? launch_dep(k_update<T, S, MJ, true, PR>, grid, dim3(UPD_THREADS), s, M, P, A, qin, qout,       \
+                               dt_update, need_dt, final_stage)                                                      \
+                  : launch_dep(k_update<T, S, MJ, false, PR>, grid, dim3(UPD_THREADS), s, M, P, A, qin, qout,      \
+                               dt_update, need_dt, final_stage)
 #define EBB_UPD(S)                                                                                                 \
     case S:                                                                                                        \
         if (M.maxJ <= 3)                                                                                           \
@@ -1479,7 +1502,7 @@ int launch_update_impl(const DMesh &M, const DPhys &P, const DArrays &A, int sta
         else if (M.maxJ == 4)                                                                                      \
             EBB_UPD_MJ(S, 4);                                                                                      \
         else                                                                                                       \
-            e = launch_dep(k_update<T, S, 6, false>, grid, dim3(UPD_THREADS), s, M, P, A, qin, qout, dt_update,    \
+            e = launch_dep(k_update<T, S, 6, false, PR>, grid, dim3(UPD_THREADS), s, M, P, A, qin, qout, dt_update,\
                            need_dt, final_stage);                                                                  \
         break;
     switch (stage) {
@@ -1499,6 +1522,32 @@ int launch_update_impl(const DMesh &M, const DPhys &P, const DArrays &A, int sta
 #undef EBB_UPD
 #undef EBB_UPD_MJ
     return ret(e);
+}
+
+// the launch-shape profile: split solves of inviscid meshes take their own shapes
+template <typename T> int shape_profile(const DPhys &P) { return (is_fp32<T> && !P.viscous) ? 1 : 0; }
+
+template <typename T>
+int launch_cell_impl(const DMesh &M, const DPhys &P, const DArrays &A, const T *qin, int limit, void *stream)
+{
+    if constexpr (is_fp32<T>)
+        if (shape_profile<T>(P)) return launch_cell_pr<T, 1>(M, P, A, qin, limit, stream);
+    return launch_cell_pr<T, 0>(M, P, A, qin, limit, stream);
+}
+template <typename T> int launch_flux_impl(const DMesh &M, const DPhys &P, const DArrays &A, const T *qin, void *stream)
+{
+    if constexpr (is_fp32<T>)
+        if (shape_profile<T>(P)) return launch_flux_pr<T, 1>(M, P, A, qin, stream);
+    return launch_flux_pr<T, 0>(M, P, A, qin, stream);
+}
+template <typename T>
+int launch_update_impl(const DMesh &M, const DPhys &P, const DArrays &A, int stage, const T *qin, T *qout,
+                       int dt_update, int need_dt, int final_stage, void *stream)
+{
+    if constexpr (is_fp32<T>)
+        if (shape_profile<T>(P))
+            return launch_update_pr<T, 1>(M, P, A, stage, qin, qout, dt_update, need_dt, final_stage, stream);
+    return launch_update_pr<T, 0>(M, P, A, stage, qin, qout, dt_update, need_dt, final_stage, stream);
 }
 
 // ---- ebb-reconstruct (app/reconstruct.d:239-424) --------------------------------
