@@ -80,11 +80,18 @@ EBB_DF_HD df operator+(df a, df b)
 }
 EBB_DF_HD df operator-(df a) { return df(-a.hi, -a.lo); }
 EBB_DF_HD df operator-(df a, df b) { return a + (-b); }
+// The product: the high words' exact product and the cross terms (four FP32
+// operations), left without the final renormalisation -- its low word may reach about
+// 1.5 units in the last place of its high word instead of 0.5.  Every operation here
+// takes such an operand: the sums and products use the low word as a correction and
+// the quotient and square root only the high word as a first approximation, so the
+// error bounds stay those of the renormalised form; comparisons of two values within
+// a unit of 2^-46 of each other may order them either way.
 EBB_DF_HD df operator*(df a, df b)
 {
     df p = two_prod(a.hi, b.hi);
     p.lo = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, p.lo));
-    return fast_two_sum(p.hi, p.lo);
+    return p;
 }
 // a double-float times an FP32 number
 EBB_DF_HD df mul_f(df a, float b)

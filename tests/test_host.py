@@ -417,7 +417,7 @@ static df rnd(int emax) {
 }
 int main() {
     const double U = 0x1p-46;
-    double emul = 0, ediv = 0, esqrt = 0, eadd = 0, eaddc = 0, econv = 0, emulf = 0;
+    double emul = 0, ediv = 0, esqrt = 0, eadd = 0, eaddc = 0, econv = 0, emulf = 0, echain = 0, edot = 0;
     long n = 0;
     for (int k = 0; k < 2000000; k++) {
         df a = rnd(20), b = rnd(20);
@@ -434,11 +434,20 @@ int main() {
         df c = -(a * df(1.0 + std::ldexp(u01(), -(int)(rng() % 40))));
         L vc = val(c);
         r = va + vc; eaddc = std::fmax(eaddc, (double)(std::fabs(val(a + c) - r) / (std::fabs(va) + std::fabs(vc))) / U);
+        // chains: a product of products, and a sum of two products (relative to the
+        // summed magnitudes)
+        df e = rnd(10);
+        L ve = val(e);
+        r = va * vb * ve;
+        echain = std::fmax(echain, (double)(std::fabs(val((a * b) * e) - r) / std::fabs(r)) / U);
+        r = va * vb + vc * ve;
+        edot = std::fmax(edot, (double)(std::fabs(val(a * b + c * e) - r) / (std::fabs(va * vb) + std::fabs(vc * ve))) / U);
         double x = std::ldexp(1.0 + u01(), (int)(rng() % 121) - 60) * ((rng() & 1) ? -1.0 : 1.0);
         econv = std::fmax(econv, (double)(std::fabs(val(df(x)) - (L)x) / std::fabs((L)x)) / U);
         n++;
     }
-    std::printf("%ld %.3f %.3f %.3f %.3f %.3f %.3f %.3f\n", n, emul, emulf, ediv, esqrt, eadd, eaddc, econv);
+    std::printf("%ld %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f %.3f\n", n, emul, emulf, ediv, esqrt, eadd, eaddc, econv,
+                echain, edot);
 }
 """
 
@@ -449,7 +458,8 @@ def test_double_float_error_bounds(tmp_path):
     over 2^+-20 of both signs: product, product by an FP32 number, quotient and square
     root within 2 units of 2^-46 of the exact result (relative); sums within 2 units of
     2^-46 of |a| + |b|, with near-cancelling pairs as well; the conversion from double
-    within 2^-48."""
+    within 2^-48; a product of products and a sum of two products (their operands not
+    renormalised) within 4 units of 2^-46 (relative to the summed magnitudes)."""
     import subprocess
     src = tmp_path / "dfcheck.cpp"
     src.write_text(DFLOAT_CHECK)
@@ -458,10 +468,11 @@ def test_double_float_error_bounds(tmp_path):
                     str(src), "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
     n = int(out[0])
-    emul, emulf, ediv, esqrt, eadd, eaddc, econv = (float(x) for x in out[1:])
+    emul, emulf, ediv, esqrt, eadd, eaddc, econv, echain, edot = (float(x) for x in out[1:])
     assert n == 2_000_000
     assert max(emul, emulf, ediv, esqrt, eadd, eaddc) <= 2.0, out
     assert econv <= 0.25, out
+    assert max(echain, edot) <= 4.0, out
 
 
 def test_hanging_node_polygons():
