@@ -1,8 +1,9 @@
 // device_math.cuh -- per-face and per-cell arithmetic of the explicit FV update,
 // templated on the arithmetic type T (double for the plain path, float for the
-// split path).  Every expression keeps the evaluation order of the D reference so
-// that, compiled without multiply-add contraction, the double instantiation rounds
-// exactly like it.  Reference lines are cited per function.
+// split path, ebbdf::df for the double-float path).  Every expression keeps the
+// evaluation order of the D reference so that, compiled without multiply-add
+// contraction, the double instantiation rounds exactly like it.  Reference lines are
+// cited per function.
 #pragma once
 
 #include <cuda_runtime.h>

@@ -5,6 +5,10 @@
 //   T = float   split path (k_split.cu): FP32 face, flux, gradient and limiter
 //               arithmetic on FP32 copies of the FP64 geometry; the solution, the
 //               u += dt R updates and the norm/force reductions stay FP64.
+//   T = df      double-float path (k_df.cu): the same arithmetic on pairs of FP32
+//               numbers (dfloat.h, ~46 bits) on double-float copies of the geometry,
+//               stage states in double-float; the solution's update in the last
+//               stage and the norm/force reductions stay FP64.
 //
 //   k_cell    one thread per interior cell: ghost states of its boundary faces
 //             (solve.d:521-689), least-squares gradient and neighbour min/max
@@ -989,10 +993,12 @@ __device__ __forceinline__ float warp_maxf(float v)
     return v;
 }
 
-// Residual of one interior cell and the stage combination.  The state update runs in
-// FP64 for both precision forms.  FP64 path: qin/qout are double stage states as in
+// Residual of one interior cell and the stage combination.  The solution's update runs
+// in FP64 for every precision form.  FP64 path: qin/qout are double stage states as in
 // integrators.d.  Split path: qin is the FP32 stage input, q64 is updated in FP64 and
-// the next stage input (qout) is its FP32 rounding.
+// the next stage input (qout) is its FP32 rounding.  Double-float path: stages before
+// the last form their stage state in double-float from the solution's double-float
+// copy; the last updates q64 in FP64 and refreshes that copy.
 template <typename T, int ST, int MJ, bool UNI, int PR>
 __global__ void __launch_bounds__(UPD_THREADS, upd_minb<T, PR>()) k_update(DMesh M, DPhys P, DArrays A, const T *__restrict__ qin, T *qout,
                                                        int dt_update, int need_dt, int final_stage)
