@@ -145,7 +145,21 @@ __device__ __forceinline__ bool pressure_negative(const double q[4])
     return pressure(q) < 0;
 }
 __device__ __forceinline__ bool pressure_negative(const float q[4]) { return pressure(q) < 0; }
-__device__ __forceinline__ bool pressure_negative(const df q[4]) { return pressure(q) < df(0.0f); }
+// Double-float: the sign of q0 q3 - 0.5 (q1^2 + q2^2) from the high words in FP32 first
+// (for q0 > 0 it is the pressure's sign).  That value is within 2^-20 of |W| + Z of
+// the double-float one (low words at most 2^-22 of the high ones, three roundings), so
+// a sign clear of 2^-17 (|W| + Z) + 2^-100 is the double-float expression's; anything
+// closer to zero, a non-positive density, NaN or overflow takes that expression.
+__device__ __forceinline__ bool pressure_negative(const df q[4])
+{
+    const float r = q[0].hi;
+    if (r > 0.0f) {
+        const float W = q[3].hi * r, Z = 0.5f * (q[1].hi * q[1].hi + q[2].hi * q[2].hi);
+        const float d = W - Z;
+        if (fabsf(d) > 0x1p-17f * (fabsf(W) + Z) + 0x1p-100f) return d < 0.0f;
+    }
+    return pressure(q) < df(0.0f);
+}
 
 // source/flux.d:19-24.  Single precision rounds every operation on its own (no
 // multiply-add contraction): the flux kernel's value for two equal face states and the
