@@ -134,9 +134,35 @@ template <typename T> __device__ __forceinline__ T pressure(const T q[4])
 // exceeds 2^-44 of its terms' magnitude (>= 32x the combined rounding bound), for
 // states within [2^-60, 2^60].  Anything closer to zero, or outside that range, takes
 // the reference's own expression, so the decision is always the reference's.
+// FP32 value of a double that is zero or in [2^-60, 2^60), its mantissa truncated to
+// 23 bits (relative error below 2^-23), from the bit pattern on the integer pipe
+__device__ __forceinline__ float trunc_f32(double x)
+{
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned mag = hi & 0x7fffffffu;
+    if ((mag | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
+    return __uint_as_float((hi & 0x80000000u) | ((mag - (896u << 20)) << 3) | (lo >> 29));
+}
+// x is zero or 2^-60 <= |x| < 2^60
+__device__ __forceinline__ bool f32_range(double x)
+{
+    const unsigned mag = (unsigned)__double2hiint(x) & 0x7fffffffu;
+    const unsigned e = mag >> 20;
+    return (mag | (unsigned)__double2loint(x)) == 0u || (e >= 1023u - 60u && e < 1023u + 60u);
+}
 __device__ __forceinline__ bool pressure_negative(const double q[4])
 {
     if (mid_range(q[0], true) && mid_range(q[3], true) && bounded(q[1]) && bounded(q[2])) {
+        if (f32_range(q[1]) && f32_range(q[2])) {
+            // first in FP32 from the truncated values: within 2^-20 of |W| + Z of the
+            // FP64 W - Z, so a sign clear of 2^-17 (|W| + Z) is that of W - Z, and with
+            // it the reference's (below); closer to zero, the FP64 test
+            const float r = trunc_f32(q[0]), e = trunc_f32(q[3]), m1 = trunc_f32(q[1]), m2 = trunc_f32(q[2]);
+            const float Wf = __fmul_rn(e, r);
+            const float Zf = __fmul_rn(0.5f, __fadd_rn(__fmul_rn(m1, m1), __fmul_rn(m2, m2)));
+            const float dd = __fsub_rn(Wf, Zf);
+            if (fabsf(dd) > 0x1p-17f * __fadd_rn(fabsf(Wf), Zf)) return dd < 0.0f;
+        }
         double W = q[3] * q[0];
         double Z = 0.5 * (q[1] * q[1] + q[2] * q[2]);
         double d = W - Z;
