@@ -143,6 +143,16 @@ __device__ __forceinline__ float trunc_f32(double x)
     if ((mag | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
     return __uint_as_float((hi & 0x80000000u) | ((mag - (896u << 20)) << 3) | (lo >> 29));
 }
+// FP32 value of any double with its mantissa truncated to 23 bits (relative error
+// below 2^-23), on the integer pipe: magnitudes below 2^-126 give a signed zero, from
+// 2^128 on (infinities and NaN included) a signed infinity
+__device__ __forceinline__ float trunc_sat(double x)
+{
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned mag = hi & 0x7fffffffu, sgn = hi & 0x80000000u;
+    const unsigned f = sgn | ((mag - (896u << 20)) << 3) | (lo >> 29);
+    return __uint_as_float(mag < (897u << 20) ? sgn : (mag >= (1151u << 20) ? (sgn | 0x7f800000u) : f));
+}
 // x is zero or 2^-60 <= |x| < 2^60
 __device__ __forceinline__ bool f32_range(double x)
 {

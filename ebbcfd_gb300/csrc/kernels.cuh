@@ -615,20 +615,55 @@ __global__ void __launch_bounds__(cell_threads<T, PR>(), cell_minb<T, PR>()) k_c
         // the busiest lane needs.  Each component's limiter still takes the minimum in
         // neighbour order (pairs in bounds give s = 1, which leaves it unchanged).
         unsigned need = 0, above = 0;
+        // FP64: each test is first taken in FP32 from the values truncated on the
+        // integer pipe (trunc_sat: within 2^-23, tiny values to zero, huge ones to
+        // infinity).  The FP32 qE is within 2^-20 of S = |q| + |g0 nx| + |g1 ny| of the
+        // FP64 one, so a side clear of 2^-18 S + 2^-100 (and 2^-20 of each bound) is
+        // the FP64 expression's; pairs closer to a bound (in uniform regions every
+        // pair), and NaN or overflowing ones, take the FP64 expression.
+        float qf[4], g0f[4], g1f[4], lof[4], hif[4];
+        if constexpr (is_fp64<T>) {
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                qf[k] = trunc_sat(qi[k]);
+                g0f[k] = trunc_sat(g[k][0]);
+                g1f[k] = trunc_sat(g[k][1]);
+                lof[k] = trunc_sat(mn[k]);
+                hif[k] = trunc_sat(mx[k]);
+            }
+        }
 #pragma unroll
         for (int j = 0; j < MJ; j++) {
             if (j < ne) {
                 const typename V2<T>::t nd = ld2<T>(M.g.s_nd, (size_t)j * Cs + i);
+                float nxf = 0.0f, nyf = 0.0f;
+                if constexpr (is_fp64<T>) {
+                    nxf = trunc_sat(nd.x);
+                    nyf = trunc_sat(nd.y);
+                }
 #pragma unroll
                 for (int k = 0; k < 4; k++) {
-                    const T qE = qi[k] + (g[k][0] * nd.x + g[k][1] * nd.y);
                     const unsigned bit = 1u << (4 * j + k);
-                    if (qE < mn[k])
-                        need |= bit;
-                    else if (qE > mx[k]) {
-                        need |= bit;
-                        above |= bit;
+                    int side = -1;
+                    if constexpr (is_fp64<T>) {
+                        const float a = __fmul_rn(g0f[k], nxf), b = __fmul_rn(g1f[k], nyf);
+                        const float e = __fadd_rn(qf[k], __fadd_rn(a, b));
+                        const float B = __fadd_rn(0x1p-18f * __fadd_rn(__fadd_rn(fabsf(qf[k]), fabsf(a)), fabsf(b)), 0x1p-100f);
+                        const float bl = __fadd_rn(0x1p-20f * fabsf(lof[k]), 0x1p-100f);
+                        const float bh = __fadd_rn(0x1p-20f * fabsf(hif[k]), 0x1p-100f);
+                        if (__fsub_rn(e, B) > __fadd_rn(lof[k], bl) && __fadd_rn(e, B) < __fsub_rn(hif[k], bh))
+                            side = 0;
+                        else if (__fadd_rn(e, B) < __fsub_rn(lof[k], bl))
+                            side = 1;
+                        else if (__fsub_rn(e, B) > __fadd_rn(hif[k], bh))
+                            side = 2;
                     }
+                    if (side < 0) {
+                        const T qE = qi[k] + (g[k][0] * nd.x + g[k][1] * nd.y);
+                        side = qE < mn[k] ? 1 : (qE > mx[k] ? 2 : 0);
+                    }
+                    if (side) need |= bit;
+                    if (side == 2) above |= bit;
                 }
             }
         }
