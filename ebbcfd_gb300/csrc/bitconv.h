@@ -48,4 +48,15 @@ EBB_HD uint32_t d2f_bits(uint32_t hi, uint32_t lo)
     return s | (((uint32_t)e << 23) + keep + up);  // a carry out of the mantissa bumps the exponent
 }
 
+// IEEE binary64 pattern -> binary32 pattern with the mantissa truncated (not rounded)
+// to 23 bits, for range filters: relative error below 2^-23 for magnitudes in
+// [2^-126, 2^128); smaller magnitudes give a signed zero, larger ones (infinities and
+// NaN included) a signed infinity.
+EBB_HD uint32_t d2f_trunc_bits(uint32_t hi, uint32_t lo)
+{
+    const uint32_t mag = hi & 0x7fffffffu, sgn = hi & 0x80000000u;
+    const uint32_t f = sgn | ((mag - (896u << 20)) << 3) | (lo >> 29);
+    return mag < (897u << 20) ? sgn : (mag >= (1151u << 20) ? (sgn | 0x7f800000u) : f);
+}
+
 }  // namespace ebbbits

@@ -12,6 +12,7 @@
 
 #include <type_traits>
 
+#include "bitconv.h"
 #include "dfloat.h"
 #include "fdiv.h"
 
@@ -134,24 +135,13 @@ template <typename T> __device__ __forceinline__ T pressure(const T q[4])
 // exceeds 2^-44 of its terms' magnitude (>= 32x the combined rounding bound), for
 // states within [2^-60, 2^60].  Anything closer to zero, or outside that range, takes
 // the reference's own expression, so the decision is always the reference's.
-// FP32 value of a double that is zero or in [2^-60, 2^60), its mantissa truncated to
-// 23 bits (relative error below 2^-23), from the bit pattern on the integer pipe
-__device__ __forceinline__ float trunc_f32(double x)
-{
-    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
-    const unsigned mag = hi & 0x7fffffffu;
-    if ((mag | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
-    return __uint_as_float((hi & 0x80000000u) | ((mag - (896u << 20)) << 3) | (lo >> 29));
-}
+
 // FP32 value of any double with its mantissa truncated to 23 bits (relative error
 // below 2^-23), on the integer pipe: magnitudes below 2^-126 give a signed zero, from
 // 2^128 on (infinities and NaN included) a signed infinity
 __device__ __forceinline__ float trunc_sat(double x)
 {
-    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
-    const unsigned mag = hi & 0x7fffffffu, sgn = hi & 0x80000000u;
-    const unsigned f = sgn | ((mag - (896u << 20)) << 3) | (lo >> 29);
-    return __uint_as_float(mag < (897u << 20) ? sgn : (mag >= (1151u << 20) ? (sgn | 0x7f800000u) : f));
+    return __uint_as_float(ebbbits::d2f_trunc_bits((unsigned)__double2hiint(x), (unsigned)__double2loint(x)));
 }
 // x is zero or 2^-60 <= |x| < 2^60
 __device__ __forceinline__ bool f32_range(double x)
@@ -167,7 +157,7 @@ __device__ __forceinline__ bool pressure_negative(const double q[4])
             // first in FP32 from the truncated values: within 2^-20 of |W| + Z of the
             // FP64 W - Z, so a sign clear of 2^-17 (|W| + Z) is that of W - Z, and with
             // it the reference's (below); closer to zero, the FP64 test
-            const float r = trunc_f32(q[0]), e = trunc_f32(q[3]), m1 = trunc_f32(q[1]), m2 = trunc_f32(q[2]);
+            const float r = trunc_sat(q[0]), e = trunc_sat(q[3]), m1 = trunc_sat(q[1]), m2 = trunc_sat(q[2]);
             const float Wf = __fmul_rn(e, r);
             const float Zf = __fmul_rn(0.5f, __fadd_rn(__fmul_rn(m1, m1), __fmul_rn(m2, m2)));
             const float dd = __fsub_rn(Wf, Zf);
