@@ -307,6 +307,20 @@ def test_server_create_fails_loudly_without_gpu():
     assert ei.value.code == 10
 
 
+def test_server_option_defaults():
+    """ebb_server_options_defaults (no device needed): split requests, finishing of
+    stalled split solves on, in plain FP64, after 1000 stalled iterations; the Python
+    mirror maps precision names for the finishing form."""
+    L = _lib.load()
+    o = _lib.ServerOptions()
+    L.ebb_server_options_defaults(C.byref(o))
+    from ebbcfd_gb300.solver import PRECISION
+    assert o.precision == PRECISION["split"] == 1
+    assert o.finish_fp64 == 1 and o.stall_steps == 1000 and o.finish_precision == PRECISION["fp64"] == 0
+    assert o.escalate == 0 and o.max_batch == 512 and o.hbm_budget == 150_000_000_000
+    assert PRECISION["df"] == 2
+
+
 def test_cylinder_generator():
     g = meshgen.cylinder(5000, seed=3)
     m = g.to_solver_mesh()
