@@ -320,8 +320,8 @@ typedef struct ebb_server_options {
                               step limit or tEnd (default 1) */
     int32_t stall_steps;   /* default 1000 */
     int32_t finish_precision; /* form of that continuation: EBB_PREC_FP64 (default) or
-                                 EBB_PREC_DF (double-float: about 2.8x FP64's speed, within
-                                 ~1e-11 of its forces) */
+                                 EBB_PREC_DF (double-float: about 4.7x FP64's speed on the
+                                 4.0M-cell viscous plate, within ~1e-10 of its forces) */
 } ebb_server_options;
 
 typedef struct ebb_request_result {
