@@ -8,7 +8,9 @@
 // functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990;
 // also J.-M. Muller et al., Handbook of Floating-Point Arithmetic, the FMA-based
 // division and reciprocal theorems):
-//   * y0 = RN32(1 / RN32(b)) (an FP32 seed, relative error < 2^-22),
+//   * y0 = RN32(1 / T32(b)) (an FP32 seed, relative error < 2^-22; T32 truncates b to
+//     FP32 and both conversions run on bit patterns -- the integer pipe on the device,
+//     where GB300 would spend FP64-unit time on conversion instructions),
 //   * two Newton steps e = 1 - b y, y = y + y e (fused), which leave y faithful,
 //   * one more such step, which makes y = RN(1/b) unless b's significand is all ones,
 //   * per numerator: q = RN(a y), r = a - b q (exact with a fused multiply-add when q
@@ -24,6 +26,8 @@
 #include <math.h>
 #include <stdint.h>
 #include <string.h>
+
+#include "bitconv.h"
 
 #if defined(__CUDACC__)
 #define EBB_FDIV_HD __host__ __device__ __forceinline__
@@ -52,7 +56,16 @@ EBB_FDIV_HD Recip recip(double b)
     Recip R{b, 0.0, false};
     const int e = exponent_of(b);
     if (e < -125 || e > 125 || (bits_of(b) & 0xfffffffffffffull) == 0xfffffffffffffull) return R;
-    double y = (double)(1.0f / (float)b);
+    const uint64_t bb = bits_of(b);
+    const uint32_t b32 = ebbbits::d2f_trunc_bits((uint32_t)(bb >> 32), (uint32_t)bb);
+    float bf;
+    memcpy(&bf, &b32, 4);
+    const float yf = 1.0f / bf;
+    uint32_t y32;
+    memcpy(&y32, &yf, 4);
+    const uint64_t y64 = ebbbits::f2d_bits(y32);
+    double y;
+    memcpy(&y, &y64, 8);
     double t = fma(-b, y, 1.0);
     y = fma(y, t, y);
     t = fma(-b, y, 1.0);
