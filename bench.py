@@ -535,7 +535,7 @@ def theory_shock_angle(M=2.5, theta_deg=15.0, g=1.4):
 
 
 def run_wedge5000(args):
-    """Accuracy of configuration 2: the 1M-cell Mach 2.5 wedge run 5000 RK2 steps in
+    """Accuracy of the wedge run: the 1M-cell Mach 2.5 wedge run 5000 RK2 steps in
     plain FP64 (bitwise equal to the oracle on the parity cases, and used here as the
     reference solution: the oracle would take ~7 min on the host), in split precision
     and in double-float; shock angle of each against the oblique-shock relation, and
@@ -582,7 +582,7 @@ def run_wedge5000(args):
 
 
 def run_plate20k(args):
-    """Configuration 3 run to its end: the 4.0M-cell Navier-Stokes plate (RK4, CFL 0.8),
+    """The Navier-Stokes plate run to its end: the 4.0M-cell plate (RK4, CFL 0.8),
     20000 steps in plain FP64 and in split precision from the same initial state, every
     step's drag and residuals recorded.  Reports each path's throughput, the drag
     coefficient Cd = drag / (0.5 rho U^2 L_w) (wall length L_w = 2, x in [0, 2]), the
